@@ -1,0 +1,626 @@
+// capi.cu — context, resident models and the C ABI (include/cudebye.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "debio.h"
+#include "engine.h"
+
+using dbx::Error;
+
+struct dbx_ctx {
+  int device = 0;
+  int num_sms = 0;
+  int hist_tasks = 0;  // histogram CTA tasks per launch
+  size_t budget = 0;  // 0 = no limit
+  size_t used = 0;    // device bytes held
+  cudaStream_t stream = nullptr;      // launch stream (own or caller's)
+  cudaStream_t own_stream = nullptr;
+  dbx::Timers tm;
+  int64_t h2d = 0, d2h = 0;           // bytes copied (dbx_get_traffic)
+  std::map<int64_t, std::unique_ptr<dbx::Model>> models;
+  int64_t next_id = 1;
+  dbx::HistWorkspace hws;
+  dbx::DevBuf tmp_hist, K, ff, I;
+  std::string last_error;
+};
+
+namespace {
+
+int set_err(dbx_ctx *c, const Error &e) {
+  if (c && e.code != DBX_OK) c->last_error = e.msg;
+  return e.code;
+}
+
+Error grow(dbx_ctx *c, dbx::DevBuf *b, size_t bytes) {
+  if (b->bytes >= bytes) return dbx::ok();
+  if (b->p) {
+    cudaFree(b->p);
+    c->used -= b->bytes;
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  if (c->budget && c->used + bytes > c->budget)
+    return dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded (" +
+                                        std::to_string(c->used + bytes) + " > " +
+                                        std::to_string(c->budget) + " bytes)");
+  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
+  b->bytes = bytes;
+  c->used += bytes;
+  return dbx::ok();
+}
+
+void release(dbx_ctx *c, dbx::DevBuf *b) {
+  if (b->p) cudaFree(b->p);
+  c->used -= b->bytes;
+  b->p = nullptr;
+  b->bytes = 0;
+}
+
+// Interleave the low 10 bits of v with two zero bits between each.
+uint32_t spread10(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+void free_model(dbx_ctx *c, dbx::Model *m) {
+  if (m->d_atoms) cudaFree(m->d_atoms);
+  if (m->d_tiles) cudaFree(m->d_tiles);
+  if (m->d_hist) cudaFree(m->d_hist);
+  c->used -= m->dev_bytes + m->hist_bytes;
+}
+
+dbx::Model *find_model(dbx_ctx *c, int64_t id) {
+  auto it = c->models.find(id);
+  return it == c->models.end() ? nullptr : it->second.get();
+}
+
+int64_t pitch_of(int64_t nbins) { return (nbins + 2 + 1) & ~int64_t(1); }
+
+// Histograms of all pairs, kept resident in the model.
+Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins) {
+  if (m->d_hist && m->hist_rstep == rstep && m->hist_nbins == nbins)
+    return dbx::ok();
+  const int np = dbx::npairs_of(m->nspecies);
+  const int64_t pitch = pitch_of(nbins);
+  const size_t bytes = sizeof(unsigned long long) * (size_t)pitch * np;
+  if (m->hist_bytes < bytes) {
+    if (m->d_hist) cudaFree(m->d_hist);
+    c->used -= m->hist_bytes;
+    m->d_hist = nullptr;
+    m->hist_bytes = 0;
+    if (c->budget && c->used + bytes > c->budget)
+      return dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by histograms");
+    DBX_CUDA_TRY(cudaMalloc(&m->d_hist, bytes));
+    m->hist_bytes = bytes;
+    c->used += bytes;
+  }
+  std::vector<int2> pairs;
+  for (int r = 0; r < m->nspecies; ++r)
+    for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
+  dbx::HistPlan plan;
+  DBX_TRY(dbx::hist_plan(*m, pairs, rstep, nbins, c->hist_tasks, &plan));
+  size_t delta = 0;
+  m->hist_rstep = 0;
+  m->hist_nbins = 0;
+  Error e = dbx::hist_run(*m, plan, (float)(1.0 / rstep), nbins, pitch,
+                          m->d_hist, &c->hws, c->stream, c->num_sms, &delta,
+                          &c->tm);
+  c->used += delta;
+  c->h2d += plan.upload_bytes();
+  c->d2h += sizeof(unsigned long long);
+  if (e.code != DBX_OK) return e;
+  m->hist_rstep = rstep;
+  m->hist_nbins = nbins;
+  m->hist_pitch = pitch;
+  return dbx::ok();
+}
+
+Error copy_rows(dbx_ctx *c, const unsigned long long *d, int64_t pitch,
+                int64_t nbins, int rows, int64_t *out) {
+  DBX_CUDA_TRY(cudaMemcpy2DAsync(out, nbins * 8, d, pitch * 8, nbins * 8, rows,
+                                 cudaMemcpyDeviceToHost, c->stream));
+  c->d2h += nbins * 8 * rows;
+  DBX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return dbx::ok();
+}
+
+Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
+                const dbx_species *sp, const double *K, int nq, int mode,
+                double *out_I) {
+  if (nq < 1) return dbx::fail(DBX_ERR_ARG, "nq must be >= 1");
+  if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_FP64 && mode != DBX_DEBYE_FP32)
+    return dbx::fail(DBX_ERR_ARG, "unknown Debye mode");
+  DBX_TRY(ensure_hist(c, m, rstep, nbins));
+  const int np = dbx::npairs_of(m->nspecies);
+  DBX_TRY(grow(c, &c->K, sizeof(double) * nq));
+  DBX_TRY(grow(c, &c->ff, sizeof(double) * nq * (size_t)np));
+  DBX_TRY(grow(c, &c->I, sizeof(double) * nq));
+  DBX_CUDA_TRY(cudaMemcpyAsync(c->K.p, K, sizeof(double) * nq,
+                               cudaMemcpyHostToDevice, c->stream));
+  c->h2d += sizeof(double) * nq + sizeof(dbx_species) * m->nspecies;
+  c->tm.start(DBX_T_PREFACTOR, c->stream);
+  DBX_TRY(dbx::debye_prefactor(sp, m->nspecies, (const double *)c->K.p, nq,
+                               (double *)c->ff.p, c->stream));
+  c->tm.stop(DBX_T_PREFACTOR, c->stream);
+  // The tensor-core form is not built yet: DBX_DEBYE_TC runs the FP64 form.
+  const int kmode = mode == DBX_DEBYE_FP32 ? DBX_DEBYE_FP32 : DBX_DEBYE_FP64;
+  c->tm.start(DBX_T_DEBYE, c->stream);
+  DBX_TRY(dbx::debye_direct(kmode, m->d_hist, np, m->hist_pitch, nbins, rstep,
+                            (const double *)c->K.p, nq,
+                            (const double *)c->ff.p, (double *)c->I.p,
+                            c->stream));
+  c->tm.stop(DBX_T_DEBYE, c->stream);
+  DBX_CUDA_TRY(cudaMemcpyAsync(out_I, c->I.p, sizeof(double) * nq,
+                               cudaMemcpyDeviceToHost, c->stream));
+  c->d2h += sizeof(double) * nq;
+  DBX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return dbx::ok();
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *dbx_strerror(int code) {
+  switch (code) {
+    case DBX_OK: return "ok";
+    case DBX_ERR_ARG: return "invalid argument";
+    case DBX_ERR_CUDA: return "CUDA error";
+    case DBX_ERR_NOMEM: return "out of memory or HBM budget";
+    case DBX_ERR_FILE: return "input file does not exist";
+    case DBX_ERR_PARSE: return "malformed .deb file";
+    case DBX_ERR_COUNT: return "atom count does not match the header";
+    case DBX_ERR_RANGE: return "distance beyond rmax";
+    case DBX_ERR_MODEL: return "unknown model id";
+    case DBX_ERR_TIMEOUT: return "device wait timed out";
+    case DBX_ERR_IO: return "output file could not be written";
+    default: return "unknown error";
+  }
+}
+
+const char *dbx_last_error(const dbx_ctx *c) {
+  return c ? c->last_error.c_str() : "no context";
+}
+
+size_t dbx_device_bytes(const dbx_ctx *c) { return c ? c->used : 0; }
+
+int dbx_create(dbx_ctx **out, int device, size_t budget) {
+  if (!out) return DBX_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+    return DBX_ERR_CUDA;
+  if (cudaSetDevice(device) != cudaSuccess) return DBX_ERR_CUDA;
+  auto c = std::make_unique<dbx_ctx>();
+  c->device = device;
+  c->budget = budget;
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount,
+                             device) != cudaSuccess)
+    return DBX_ERR_CUDA;
+  // Tasks per histogram launch: 2 per SM by default. DBX_HIST_TASKS
+  // overrides it (tuning; fewer tasks also means more counts per task).
+  c->hist_tasks = 2 * c->num_sms;
+  if (const char *v = getenv("DBX_HIST_TASKS")) {
+    const int t = atoi(v);
+    if (t > 0) c->hist_tasks = t;
+  }
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) !=
+      cudaSuccess)
+    return DBX_ERR_CUDA;
+  c->stream = c->own_stream;
+  *out = c.release();
+  return DBX_OK;
+}
+
+int dbx_destroy(dbx_ctx *c) {
+  if (!c) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->models) free_model(c, kv.second.get());
+  c->models.clear();
+  release(c, &c->hws.items);
+  release(c, &c->hws.segs);
+  release(c, &c->hws.tasks);
+  release(c, &c->hws.partial);
+  release(c, &c->hws.oor);
+  release(c, &c->tmp_hist);
+  release(c, &c->K);
+  release(c, &c->ff);
+  release(c, &c->I);
+  if (c->tm.created)
+    for (auto &p : c->tm.ev) {
+      cudaEventDestroy(p[0]);
+      cudaEventDestroy(p[1]);
+    }
+  cudaStreamDestroy(c->own_stream);
+  delete c;
+  return DBX_OK;
+}
+
+int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
+                     const float *z, const int64_t *counts, int nspecies,
+                     int64_t *model_id) {
+  if (!c || !counts || nspecies < 1 || !model_id) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  int64_t natoms = 0;
+  for (int s = 0; s < nspecies; ++s) {
+    if (counts[s] < 0) return set_err(c, dbx::fail(DBX_ERR_ARG, "negative species count"));
+    natoms += counts[s];
+  }
+  if (natoms > 0 && (!x || !y || !z))
+    return set_err(c, dbx::fail(DBX_ERR_ARG, "null coordinate array"));
+  if (natoms >= (int64_t(1) << 31))
+    return set_err(c, dbx::fail(DBX_ERR_ARG, "more than 2^31 atoms"));
+  auto m = std::make_unique<dbx::Model>();
+  m->nspecies = nspecies;
+  m->natoms = natoms;
+  // Morton order on a 1024^3 grid over the model's bounding cube.
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  const float *xyz[3] = {x, y, z};
+  for (int64_t i = 0; i < natoms; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const float v = xyz[d][i];
+      if (v < lo[d]) lo[d] = v;
+      if (v > hi[d]) hi[d] = v;
+    }
+  float ext = 0;
+  for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
+  const double scale = ext > 0 ? 1023.0 / ext : 0.0;
+  std::vector<float4> atoms(std::max<int64_t>(natoms, 1));
+  std::vector<uint32_t> code;
+  std::vector<int64_t> idx;
+  int64_t start = 0;
+  m->tile_start.push_back(0);
+  for (int s = 0; s < nspecies; ++s) {
+    const int64_t n = counts[s];
+    code.resize(n);
+    idx.resize(n);
+    for (int64_t i = 0; i < n; ++i) {
+      uint32_t q[3];
+      for (int d = 0; d < 3; ++d) {
+        double t = ((double)xyz[d][start + i] - lo[d]) * scale;
+        t = std::isfinite(t) ? std::min(std::max(t, 0.0), 1023.0) : 0.0;
+        q[d] = (uint32_t)t;
+      }
+      code[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+      idx[i] = i;
+    }
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int64_t a, int64_t b) { return code[a] < code[b]; });
+    for (int64_t i = 0; i < n; ++i) {
+      const int64_t src = start + idx[i];
+      atoms[start + i] = make_float4(x[src], y[src], z[src], 0.f);
+    }
+    m->sp_start.push_back(start);
+    m->sp_count.push_back(n);
+    for (int64_t t0 = 0; t0 < n; t0 += dbx::kTile) {
+      const int cnt = (int)std::min<int64_t>(dbx::kTile, n - t0);
+      m->tiles.push_back(make_int2((int)(start + t0), cnt));
+      dbx::TileBox b;
+      for (int d = 0; d < 3; ++d) {
+        b.lo[d] = INFINITY;
+        b.hi[d] = -INFINITY;
+      }
+      for (int i = 0; i < cnt; ++i) {
+        const float4 a = atoms[start + t0 + i];
+        const float v[3] = {a.x, a.y, a.z};
+        for (int d = 0; d < 3; ++d) {
+          b.lo[d] = std::min(b.lo[d], v[d]);
+          b.hi[d] = std::max(b.hi[d], v[d]);
+        }
+      }
+      m->boxes.push_back(b);
+    }
+    m->tile_start.push_back((int)m->tiles.size());
+    start += n;
+  }
+  const size_t abytes = sizeof(float4) * atoms.size();
+  const size_t tbytes = sizeof(int2) * std::max<size_t>(m->tiles.size(), 1);
+  if (c->budget && c->used + abytes + tbytes > c->budget)
+    return set_err(c, dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by model"));
+  if (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
+      cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess) {
+    free_model(c, m.get());
+    return set_err(c, dbx::fail(DBX_ERR_NOMEM, "cudaMalloc failed for model"));
+  }
+  m->dev_bytes = abytes + tbytes;
+  c->used += m->dev_bytes;
+  Error e = dbx::ok();
+  if (cudaMemcpy(m->d_atoms, atoms.data(), abytes, cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      (m->tiles.size() &&
+       cudaMemcpy(m->d_tiles, m->tiles.data(), sizeof(int2) * m->tiles.size(),
+                  cudaMemcpyHostToDevice) != cudaSuccess))
+    e = dbx::fail(DBX_ERR_CUDA, "model upload copy failed");
+  if (e.code != DBX_OK) {
+    free_model(c, m.get());
+    return set_err(c, e);
+  }
+  c->h2d += abytes + sizeof(int2) * m->tiles.size();
+  m->id = c->next_id++;
+  *model_id = m->id;
+  c->models[m->id] = std::move(m);
+  return DBX_OK;
+}
+
+int dbx_model_free(dbx_ctx *c, int64_t id) {
+  if (!c) return DBX_ERR_ARG;
+  auto it = c->models.find(id);
+  if (it == c->models.end()) return DBX_ERR_MODEL;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_model(c, it->second.get());
+  c->models.erase(it);
+  return DBX_OK;
+}
+
+int64_t dbx_channels(double rmax, double rstep) {
+  return (int64_t)(int)(rmax / rstep) + 2;  // cuDebye-v15.cu:732
+}
+
+int dbx_pair_histogram(dbx_ctx *c, int64_t id, int row, int col, double rstep,
+                       int64_t nbins, int64_t *out) {
+  if (!c || !out || !(rstep > 0)) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  dbx::Model *m = find_model(c, id);
+  if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
+  if (row < 0 || col < row || col >= m->nspecies)
+    return set_err(c, dbx::fail(DBX_ERR_ARG, "need 0 <= row <= col < nspecies"));
+  dbx::HistPlan plan;
+  Error e = dbx::hist_plan(*m, {make_int2(row, col)}, rstep, nbins,
+                           c->hist_tasks, &plan);
+  if (e.code) return set_err(c, e);
+  const int64_t pitch = pitch_of(nbins);
+  e = grow(c, &c->tmp_hist, sizeof(unsigned long long) * pitch);
+  if (e.code) return set_err(c, e);
+  size_t delta = 0;
+  c->tm.reset();
+  e = dbx::hist_run(*m, plan, (float)(1.0 / rstep), nbins, pitch,
+                    (unsigned long long *)c->tmp_hist.p, &c->hws, c->stream,
+                    c->num_sms, &delta, &c->tm);
+  c->used += delta;
+  c->h2d += plan.upload_bytes();
+  c->d2h += sizeof(unsigned long long);
+  if (e.code) return set_err(c, e);
+  return set_err(c, copy_rows(c, (const unsigned long long *)c->tmp_hist.p,
+                              pitch, nbins, 1, out));
+}
+
+int dbx_histogram(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
+                  int64_t *out) {
+  if (!c || !out || !(rstep > 0)) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  dbx::Model *m = find_model(c, id);
+  if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
+  c->tm.reset();
+  Error e = ensure_hist(c, m, rstep, nbins);
+  if (e.code) return set_err(c, e);
+  return set_err(c, copy_rows(c, m->d_hist, m->hist_pitch, nbins,
+                              dbx::npairs_of(m->nspecies), out));
+}
+
+int dbx_reduce_check(const int64_t *counts, int64_t nbins, double rstep,
+                     int64_t n_row, int64_t n_col, int diag, int64_t out[4]) {
+  if (!counts || !out || nbins < 1) return DBX_ERR_ARG;
+  // cuDebye-v15.cu:369-409
+  int64_t expected = diag ? (n_col * n_row - n_row) / 2 + n_col : n_col * n_row;
+  int64_t observed = 0, below = 0;
+  for (int64_t k = 0; k < nbins; ++k) {
+    observed += counts[k];
+    if ((double)k * rstep < 0.25) below += counts[k];
+  }
+  out[0] = expected;
+  out[1] = observed;
+  out[2] = counts[0];
+  out[3] = diag ? std::max<int64_t>(0, below - n_col) : below;
+  return DBX_OK;
+}
+
+int dbx_k_grid(double lambda, double tt_min, double tt_max, double tt_step,
+               double *two_theta, double *K) {
+  if (!(tt_step > 0) || !(lambda > 0)) return DBX_ERR_ARG;
+  const int n = (int)((tt_max - tt_min) / tt_step) + 1;  // cuDebye-v15.cu:690
+  if (n < 1) return DBX_ERR_ARG;
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    const double tt = tt_min + (double)i * tt_step;
+    if (two_theta) two_theta[i] = tt;
+    if (K) K[i] = 4 * pi * sin(tt / 2 * pi / 180) / lambda;  // :697
+  }
+  return n;
+}
+
+int dbx_atomic_prop(dbx_ctx *c, const dbx_species *a, const dbx_species *b,
+                    const double *K, int nq, double *out_ff) {
+  if (!c || !a || !b || !K || !out_ff || nq < 1) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  dbx_species sp[2] = {*a, *b};
+  // pair (0,1) of a 2-species list is index 1
+  Error e = grow(c, &c->K, sizeof(double) * nq);
+  if (!e.code) e = grow(c, &c->ff, sizeof(double) * nq * 3);
+  if (e.code) return set_err(c, e);
+  if (cudaMemcpyAsync(c->K.p, K, sizeof(double) * nq, cudaMemcpyHostToDevice,
+                      c->stream) != cudaSuccess)
+    return set_err(c, dbx::fail(DBX_ERR_CUDA, "copy K"));
+  e = dbx::debye_prefactor(sp, 2, (const double *)c->K.p, nq,
+                           (double *)c->ff.p, c->stream);
+  if (e.code) return set_err(c, e);
+  if (cudaMemcpyAsync(out_ff, (double *)c->ff.p + nq, sizeof(double) * nq,
+                      cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return set_err(c, dbx::fail(DBX_ERR_CUDA, "copy ff"));
+  return DBX_OK;
+}
+
+int dbx_intensity(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
+                  const dbx_species *sp, const double *K, int nq, int mode,
+                  double *out_I) {
+  if (!c || !sp || !K || !out_I || !(rstep > 0)) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  dbx::Model *m = find_model(c, id);
+  if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
+  c->tm.reset();
+  return set_err(c, intensity(c, m, rstep, nbins, sp, K, nq, mode, out_I));
+}
+
+int dbx_pattern(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
+                const dbx_species *sp, const double *K, int nq, int mode,
+                double *out_I) {
+  if (!c || !sp || !K || !out_I || !(rstep > 0)) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  dbx::Model *m = find_model(c, id);
+  if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
+  c->tm.reset();
+  m->hist_nbins = 0;  // recompute the histograms: one full pattern
+  return set_err(c, intensity(c, m, rstep, nbins, sp, K, nq, mode, out_I));
+}
+
+int dbx_set_stream(dbx_ctx *c, void *stream) {
+  if (!c) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return DBX_OK;
+}
+
+int dbx_set_timing(dbx_ctx *c, int enable) {
+  if (!c) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (enable && !c->tm.created) {
+    for (auto &p : c->tm.ev)
+      if (cudaEventCreate(&p[0]) != cudaSuccess ||
+          cudaEventCreate(&p[1]) != cudaSuccess)
+        return DBX_ERR_CUDA;
+    c->tm.created = true;
+  }
+  c->tm.on = enable != 0;
+  c->tm.reset();
+  return DBX_OK;
+}
+
+int dbx_get_traffic(const dbx_ctx *c, int64_t out[2]) {
+  if (!c || !out) return DBX_ERR_ARG;
+  out[0] = c->h2d;
+  out[1] = c->d2h;
+  return DBX_OK;
+}
+
+int dbx_get_timing(const dbx_ctx *c, double out_ms[DBX_NTIMERS]) {
+  if (!c || !out_ms) return DBX_ERR_ARG;
+  for (int i = 0; i < DBX_NTIMERS; ++i) {
+    out_ms[i] = 0.0;
+    if (c->tm.created && c->tm.recorded[i]) {
+      float ms = 0.f;
+      if (cudaEventSynchronize(c->tm.ev[i][1]) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, c->tm.ev[i][0], c->tm.ev[i][1]) !=
+              cudaSuccess)
+        return DBX_ERR_CUDA;
+      out_ms[i] = ms;
+    }
+  }
+  return DBX_OK;
+}
+
+int dbx_run_deb(dbx_ctx *c, const char *deb_path, const char *out_prefix,
+                int verbose) {
+  if (!c || !deb_path) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  dbx::DebFile d;
+  std::string msg;
+  int rc = dbx::deb_read(deb_path, &d, &msg);
+  if (rc) {
+    c->last_error = msg;
+    if (verbose) printf("\nERROR: %s\n", msg.c_str());
+    return rc;
+  }
+  const std::string prefix = out_prefix ? out_prefix : deb_path;
+  const int P = (int)d.species.size();
+  std::vector<int64_t> counts(P);
+  std::vector<dbx_species> sp(P);
+  for (int i = 0; i < P; ++i) {
+    counts[i] = d.species[i].n;
+    sp[i] = d.species[i].p;
+  }
+  int64_t id = 0;
+  rc = dbx_model_upload(c, d.x.data(), d.y.data(), d.z.data(), counts.data(), P,
+                        &id);
+  if (rc) return rc;
+  struct Drop {
+    dbx_ctx *c;
+    int64_t id;
+    ~Drop() { dbx_model_free(c, id); }
+  } drop{c, id};
+  const int64_t nbins = dbx_channels(d.rmax, d.rstep);
+  dbx::Model *m = find_model(c, id);
+  Error e = ensure_hist(c, m, d.rstep, nbins);
+  if (e.code) {
+    if (verbose) printf("\nERROR: %s\n", e.msg.c_str());
+    return set_err(c, e);
+  }
+  if (d.hist > 0 || verbose) {
+    std::vector<int64_t> h(nbins);
+    for (int row = 0; row < P; ++row)
+      for (int col = row; col < P; ++col) {
+        const int p = dbx::pair_index(P, row, col);
+        e = copy_rows(c, m->d_hist + (size_t)p * m->hist_pitch, m->hist_pitch,
+                      nbins, 1, h.data());
+        if (e.code) return set_err(c, e);
+        if (verbose) {
+          int64_t chk[4];
+          dbx_reduce_check(h.data(), nbins, d.rstep, counts[row], counts[col],
+                           row == col, chk);
+          printf("\n>>>> Subgroup %d and %d\n", row, col);
+          if (chk[0] != chk[1])
+            printf("WARNING: %lld Distances Expected and %lld Observed!!!\n",
+                   (long long)chk[0], (long long)chk[1]);
+          if (row == col && chk[2] != counts[row])
+            printf("WARNING: Number of Expected Zero Distances Missing or not "
+                   "Correct!!!\n");
+          if (chk[3] > 0)
+            printf("WARNING: Possible Atom Collision!!! Found around %lld "
+                   "interatomic Distances lower than the Radius of an Hydrogen "
+                   "Atom.\n",
+                   (long long)chk[3]);
+          printf("Distances Expected: %lld - Distances Observed: %lld\n",
+                 (long long)chk[0], (long long)chk[1]);
+        }
+        if (d.hist > 0) {
+          const std::string path =
+              prefix + "x" + std::to_string(row) + "x" + std::to_string(col);
+          if (dbx::write_debx(path, h.data(), nbins, d.rstep))
+            return set_err(c, dbx::fail(DBX_ERR_IO, "cannot write " + path));
+        }
+      }
+  }
+  if (d.hist != 1) {
+    const int nq = dbx_k_grid(d.lambda, d.tt_min, d.tt_max, d.tt_step, nullptr,
+                              nullptr);
+    if (nq < 1) return set_err(c, dbx::fail(DBX_ERR_PARSE, "empty 2theta grid"));
+    std::vector<double> tt(nq), K(nq), I(nq);
+    dbx_k_grid(d.lambda, d.tt_min, d.tt_max, d.tt_step, tt.data(), K.data());
+    e = intensity(c, m, d.rstep, nbins, sp.data(), K.data(), nq, DBX_DEBYE_TC,
+                  I.data());
+    if (e.code) return set_err(c, e);
+    const std::string path = prefix + "I";
+    if (dbx::write_debI(path, tt.data(), I.data(), nq))
+      return set_err(c, dbx::fail(DBX_ERR_IO, "cannot write " + path));
+    if (verbose) printf("\nWrote %s (%d points)\n", path.c_str(), nq);
+  }
+  return DBX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,160 @@
+// debye.cu — Debye sum kernels on sm_103a (hot path 2, direct forms).
+//
+//  * debye_prefactor_kernel: the reference's atomicScatter
+//    (cuDebye-v15.cu:447-467), one thread per (pair, q), FP64.
+//  * debye_direct_kernel<T>: the reference's debyeRowSum arithmetic
+//    (cuDebye-v15.cu:493-538) for all pairs of a model at once: one thread
+//    per q, bins staged through shared memory, sinc evaluated once per
+//    (q, bin) and shared by every pair. T = double is the FP64 form; T =
+//    float is the plain unbatched FP32 GPU form used as the speed baseline.
+//    Zero bins are skipped, as the reference's compaction does
+//    (cuDebye-v15.cu:323-333).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "engine.h"
+
+namespace dbx {
+
+struct SpeciesDev {
+  double occ, beq, a[5], b[5], c;
+};
+
+__global__ void debye_prefactor_kernel(const SpeciesDev *__restrict__ sp,
+                                       int nspecies,
+                                       const double *__restrict__ K, int nq,
+                                       double *__restrict__ ff) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  if (q >= nq) return;
+  // pair index -> (row, col) in the reference's loop order (:941-942)
+  int row = 0, rem = p;
+  while (rem >= nspecies - row) {
+    rem -= nspecies - row;
+    ++row;
+  }
+  const int col = row + rem;
+  const SpeciesDev &s1 = sp[row], &s2 = sp[col];
+  const double rp16pi2 = -0.006332573977646;  // cuDebye-v15.cu:452
+  const double nhs = K[q] * K[q] * rp16pi2;
+  double v = s1.occ * s2.occ;
+  v = v * exp(nhs * (s1.beq + s2.beq));
+  double f1 = s1.c, f2 = s2.c;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    f1 += s1.a[i] * exp(s1.b[i] * nhs);
+    f2 += s2.a[i] * exp(s2.b[i] * nhs);
+  }
+  ff[(size_t)p * nq + q] = v * f1 * f2;
+}
+
+Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
+                      int nq, double *d_ff, cudaStream_t stream) {
+  static_assert(sizeof(SpeciesDev) == sizeof(dbx_species), "layout");
+  SpeciesDev *d_sp = nullptr;
+  DBX_CUDA_TRY(cudaMallocAsync((void **)&d_sp, sizeof(SpeciesDev) * nspecies,
+                               stream));
+  DBX_CUDA_TRY(cudaMemcpyAsync(d_sp, sp, sizeof(SpeciesDev) * nspecies,
+                               cudaMemcpyHostToDevice, stream));
+  dim3 grid((nq + 127) / 128, npairs_of(nspecies));
+  debye_prefactor_kernel<<<grid, 128, 0, stream>>>(d_sp, nspecies, d_K, nq,
+                                                   d_ff);
+  cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(d_sp, stream);
+  if (e != cudaSuccess)
+    return fail(DBX_ERR_CUDA, std::string("prefactor: ") + cudaGetErrorString(e));
+  return ok();
+}
+
+constexpr int kDirectThreads = 128;
+constexpr int kDirectChunk = 128;  // bins staged per shared-memory round
+constexpr int kDirectMaxPairs = 16;
+
+template <typename T>
+__device__ __forceinline__ T sinc_term(T kr);
+template <>
+__device__ __forceinline__ double sinc_term<double>(double kr) {
+  return sin(kr) / kr;
+}
+template <>
+__device__ __forceinline__ float sinc_term<float>(float kr) {
+  return sinf(kr) / kr;
+}
+
+// I[q] += sum_{p < np} ff[p0+p][q] * sum_k m_kp sinc(K_q r_k).
+template <typename T>
+__global__ void __launch_bounds__(kDirectThreads)
+    debye_direct_kernel(const unsigned long long *__restrict__ hist,
+                        int p0, int np, long long pitch, int nbins,
+                        double rstep, const double *__restrict__ K, int nq,
+                        const double *__restrict__ ff, double *__restrict__ I) {
+  __shared__ T s_m[kDirectMaxPairs][kDirectChunk];
+  __shared__ T s_r[kDirectChunk];
+  __shared__ int s_kind[kDirectChunk];  // 0 zero bin, 1 self (r<=0.0005), 2 sinc
+  const int q = blockIdx.x * kDirectThreads + threadIdx.x;
+  const T Kq = (T)K[q < nq ? q : nq - 1];
+  T acc[kDirectMaxPairs];
+#pragma unroll
+  for (int p = 0; p < kDirectMaxPairs; ++p) acc[p] = 0;
+  for (int k0 = 0; k0 < nbins; k0 += kDirectChunk) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDirectChunk; i += kDirectThreads) {
+      const int k = k0 + i;
+      const double r = (double)k * rstep;  // r_reduced (cuDebye-v15.cu:735)
+      int any = 0;
+      for (int p = 0; p < np; ++p) {
+        const unsigned long long n =
+            k < nbins ? hist[(long long)(p0 + p) * pitch + k] : 0ull;
+        any |= n != 0;
+        // m = 2n off the self distance, n on it (cuDebye-v15.cu:508-514)
+        s_m[p][i] = (T)(r > 0.0005 ? 2.0 * (double)n : (double)n);
+      }
+      s_r[i] = (T)r;
+      s_kind[i] = any ? (r > 0.0005 ? 2 : 1) : 0;
+    }
+    __syncthreads();
+    for (int i = 0; i < kDirectChunk; ++i) {
+      const int kind = s_kind[i];
+      if (kind == 0) continue;
+      const T sc = kind == 2 ? sinc_term<T>(Kq * s_r[i]) : (T)1;
+#pragma unroll
+      for (int p = 0; p < kDirectMaxPairs; ++p)
+        if (p < np) {
+          const T m = s_m[p][i];
+          if (m != (T)0) acc[p] += m * sc;
+        }
+    }
+  }
+  if (q < nq) {
+    double s = I[q];
+#pragma unroll
+    for (int p = 0; p < kDirectMaxPairs; ++p)
+      if (p < np) s += (double)acc[p] * ff[(size_t)(p0 + p) * nq + q];
+    I[q] = s;
+  }
+}
+
+Error debye_direct(int mode, const unsigned long long *d_hist, int npairs,
+                   int64_t pitch, int64_t nbins, double rstep,
+                   const double *d_K, int nq, const double *d_ff, double *d_I,
+                   cudaStream_t stream) {
+  DBX_CUDA_TRY(cudaMemsetAsync(d_I, 0, sizeof(double) * nq, stream));
+  const int grid = (nq + kDirectThreads - 1) / kDirectThreads;
+  for (int p0 = 0; p0 < npairs; p0 += kDirectMaxPairs) {
+    const int np = std::min(kDirectMaxPairs, npairs - p0);
+    if (mode == DBX_DEBYE_FP32)
+      debye_direct_kernel<float><<<grid, kDirectThreads, 0, stream>>>(
+          d_hist, p0, np, (long long)pitch, (int)nbins, rstep, d_K, nq, d_ff,
+          d_I);
+    else
+      debye_direct_kernel<double><<<grid, kDirectThreads, 0, stream>>>(
+          d_hist, p0, np, (long long)pitch, (int)nbins, rstep, d_K, nq, d_ff,
+          d_I);
+    DBX_CUDA_TRY(cudaGetLastError());
+  }
+  return ok();
+}
+
+}  // namespace dbx

@@ -1,0 +1,157 @@
+// engine.h — internal declarations of the GB300 Debye engine (not part of
+// the C ABI; see include/cudebye.h for that).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cudebye.h"
+
+namespace dbx {
+
+// ---- error plumbing ------------------------------------------------------
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define DBX_CUDA_TRY(expr)                                                   \
+  do {                                                                       \
+    cudaError_t e_ = (expr);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return ::dbx::Error{DBX_ERR_CUDA,                                      \
+                          std::string(#expr) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+
+#define DBX_TRY(expr)                  \
+  do {                                 \
+    ::dbx::Error e_ = (expr);          \
+    if (e_.code != DBX_OK) return e_;  \
+  } while (0)
+
+inline Error ok() { return Error{DBX_OK, std::string()}; }
+inline Error fail(int code, const std::string &m) { return Error{code, m}; }
+
+// ---- phase timers ----------------------------------------------------------
+// CUDA-event timing of the phases of a call, on the launching stream.
+struct Timers {
+  bool on = false;
+  bool created = false;
+  cudaEvent_t ev[DBX_NTIMERS][2];
+  bool recorded[DBX_NTIMERS] = {false, false, false, false};
+  void reset() {
+    for (bool &r : recorded) r = false;
+  }
+  void start(int i, cudaStream_t s) {
+    if (on) {
+      cudaEventRecord(ev[i][0], s);
+      recorded[i] = true;
+    }
+  }
+  void stop(int i, cudaStream_t s) {
+    if (on) cudaEventRecord(ev[i][1], s);
+  }
+};
+
+// ---- device buffers -------------------------------------------------------
+// Growable device buffer owned by a context; memory is accounted against the
+// context's HBM budget by the owner.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+// ---- resident model -------------------------------------------------------
+// Atoms are stored per species, each species sorted along a Morton curve
+// and cut into tiles of kTile atoms, so that a tile is spatially compact and
+// a tile pair covers a narrow window of distances.
+constexpr int kTile = 128;
+
+struct TileBox {
+  float lo[3], hi[3];
+};
+
+struct Model {
+  int64_t id = 0;
+  int nspecies = 0;
+  int64_t natoms = 0;
+  std::vector<int64_t> sp_start, sp_count;  // in atoms (sorted layout)
+  std::vector<int> tile_start;              // first tile of each species (+ end)
+  std::vector<int2> tiles;                  // {first atom, count}
+  std::vector<TileBox> boxes;               // per tile, host only
+  float4 *d_atoms = nullptr;                // natoms x (x, y, z, 0)
+  int2 *d_tiles = nullptr;
+  size_t dev_bytes = 0;
+  // Resident histograms (for re-scoring with new K or species).
+  double hist_rstep = 0;
+  int64_t hist_nbins = 0;
+  int64_t hist_pitch = 0;                 // nbins padded, in int64
+  unsigned long long *d_hist = nullptr;   // [npairs][pitch]
+  size_t hist_bytes = 0;
+};
+
+inline int npairs_of(int p) { return p * (p + 1) / 2; }
+inline int pair_index(int p, int row, int col) {
+  return row * p - row * (row - 1) / 2 + (col - row);
+}
+
+// ---- histogram planner + kernels (hist.cu) --------------------------------
+struct HistSeg {  // one (pair, bin window) accumulated in shared memory
+  int pair;       // output row
+  int kb;         // first bin of the window
+  int wl;         // window length in bins
+  int task_begin, task_end;
+};
+struct HistTask {  // one CTA-sized slice of a segment's tile pairs
+  int seg;
+  int item_begin, item_end;
+  int pad;
+};
+
+struct HistPlan {
+  std::vector<int2> items;  // {tile I, tile J | (diag << 31)}
+  std::vector<HistSeg> segs;
+  std::vector<HistTask> tasks;
+  int window = 0;           // bins per shared-memory window
+  int nrows = 0;            // output histograms (selected pairs)
+  int64_t pairs = 0;        // binned pairs (the reference's "Distances
+                            // Expected" summed over the selected pairs)
+  size_t upload_bytes() const {
+    return items.size() * sizeof(int2) + segs.size() * sizeof(HistSeg) +
+           tasks.size() * sizeof(HistTask);
+  }
+};
+
+// Plan the histogram of the selected pairs (list of (row, col)), cut into
+// about target_tasks CTA tasks of equal pair counts.
+Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
+                int64_t nbins, int target_tasks, HistPlan *plan);
+
+struct HistWorkspace {  // device-side scratch for one histogram run
+  DevBuf items, segs, tasks, partial, oor;
+};
+
+// Run a plan: out = device int64 histograms [plan.nrows][pitch], zeroed
+// here; pitch >= nbins + 2 (the two bins past the end absorb the carry
+// bookkeeping of the packed counters). Returns DBX_ERR_RANGE if any pair binned at k >= nbins.
+Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
+               int64_t nbins, int64_t pitch, unsigned long long *d_out,
+               HistWorkspace *ws, cudaStream_t stream, int num_sms,
+               size_t *ws_bytes_delta, Timers *tm);
+
+int hist_window_bins();  // shared-memory window capacity in bins
+
+// ---- Debye kernels (debye.cu) ----------------------------------------------
+// out_ff[p][q] for every pair of the model's species.
+Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
+                      int nq, double *d_ff, cudaStream_t stream);
+// I[q] = sum_p ff[p][q] * sum_k m_k sinc(K r_k) over the model's histograms.
+Error debye_direct(int mode, const unsigned long long *d_hist, int npairs,
+                   int64_t pitch, int64_t nbins, double rstep,
+                   const double *d_K, int nq, const double *d_ff, double *d_I,
+                   cudaStream_t stream);
+
+}  // namespace dbx

@@ -1,0 +1,358 @@
+// hist.cu — all-pairs distance histogram on sm_103a (hot path 1).
+//
+// Replaces the reference's splitCalcDist and its kernels dist / dist2 /
+// care_dist2 (cuDebye-v15.cu:88-272), which bin every pair with a global
+// uint32 atomicAdd and synchronise the host after every 67M-pair launch.
+//
+// Design:
+//  * Atoms of each species are Morton-sorted and cut into tiles of 128
+//    (capi.cu); a work item is one tile pair.
+//  * A CTA owns a window of up to ~114k bins held in shared memory as packed
+//    16-bit counters (two bins per 32-bit word). A counter that wraps is
+//    detected from the atomic's return value and compensated exactly in the
+//    int64 global histogram (see add16), so the counts stay exact.
+//  * Tile pairs are grouped into (species pair, bin window) segments from
+//    their bounding boxes, and split into equal CTA tasks. Each task writes
+//    its packed window once to a scratch slot; a reduce kernel sums the slots
+//    of a segment into the int64 histogram. No host round trip between tiles.
+//  * The distance and bin are the reference's FP32 formula, unfused
+//    (cuDebye-v15.cu:101-107): IEEE sqrt, explicit _rn intrinsics so that
+//    nothing is contracted to FMA, and roundf computed exactly without a
+//    float->int conversion (exact_bin).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "engine.h"
+
+namespace dbx {
+
+constexpr int kHistThreads = 1024;
+// Dynamic shared memory per CTA for the window (bytes); 1 CTA per SM.
+constexpr int kHistSmemBytes = 224 * 1024;
+constexpr int kWindowBins = (kHistSmemBytes / 4) * 2;  // 114688, even
+
+int hist_window_bins() { return kWindowBins; }
+
+// Exact bin of one pair: (int)roundf(sqrtf((dx*dx + dy*dy) + dz*dz) * inv)
+// with every operation rounded separately (cuDebye-v15.cu:101-107, :115).
+// roundf(p) for 0 <= p < 2^23: t = p + 2^23 rounds p to an integer with
+// ties-to-even; the bits of t minus those of 2^23 are that integer; a tie
+// (p - round_even(p) == 0.5) is moved up, giving round-half-away-from-zero.
+// p >= 2^23, inf or NaN give an index >= 2^23 (or negative), which the
+// caller treats as out of range.
+__device__ __forceinline__ int exact_bin(float ax, float ay, float az,
+                                         float4 b, float inv) {
+  const float dx = __fsub_rn(b.x, ax);
+  const float dy = __fsub_rn(b.y, ay);
+  const float dz = __fsub_rn(b.z, az);
+  float s = __fmul_rn(dx, dx);
+  s = __fadd_rn(s, __fmul_rn(dy, dy));
+  s = __fadd_rn(s, __fmul_rn(dz, dz));
+  const float p = __fmul_rn(__fsqrt_rn(s), inv);
+  const float t = __fadd_rn(p, 8388608.0f);
+  int k = __float_as_int(t) - 0x4B000000;
+  const float r = __fsub_rn(t, 8388608.0f);
+  k += (__fsub_rn(p, r) == 0.5f) ? 1 : 0;
+  return k;
+}
+
+// Add one count to bin lk of the packed 16-bit shared window. When the add
+// wraps a 16-bit half (seen in the returned old value), credit 65536 to that
+// bin in the global int64 histogram; a wrap of the low half also carried 1
+// into the high half (bin lk+1), which is debited there, and if that carry
+// wrapped the high half as well it is credited too. Every wrap is seen by
+// exactly one thread (the one whose atomic caused it), so
+// count = stored + 65536*wraps - carries holds exactly.
+__device__ __forceinline__ void add16(unsigned *sh, unsigned lk,
+                                      unsigned long long *gh) {
+  const unsigned sh16 = (lk & 1u) << 4;
+  const unsigned old = atomicAdd(&sh[lk >> 1], 1u << sh16);
+  if (((old >> sh16) & 0xFFFFu) == 0xFFFFu) {
+    atomicAdd(&gh[lk], 65536ull);
+    if (sh16 == 0) {
+      atomicAdd(&gh[lk + 1], ~0ull);  // -1 for the carry
+      if ((old >> 16) == 0xFFFFu) atomicAdd(&gh[lk + 1], 65536ull);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kHistThreads, 1)
+    hist_tiles_kernel(const float4 *__restrict__ atoms,
+                      const int2 *__restrict__ tiles,
+                      const int2 *__restrict__ items,
+                      const HistTask *__restrict__ tasks, int ntasks,
+                      const HistSeg *__restrict__ segs, float inv,
+                      unsigned nbins, unsigned *__restrict__ partial,
+                      int words_per_task, unsigned long long *__restrict__ hist,
+                      long long pitch,
+                      unsigned long long *__restrict__ oor_total) {
+  extern __shared__ unsigned sh[];
+  __shared__ unsigned s_oor;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kSub = kTile / 32;  // warp sub-blocks per tile
+  for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const HistTask tk = tasks[t];
+    const HistSeg sg = segs[tk.seg];
+    const int nw = (sg.wl + 1) >> 1;
+    for (int i = threadIdx.x; i < nw; i += kHistThreads) sh[i] = 0u;
+    if (threadIdx.x == 0) s_oor = 0u;
+    __syncthreads();
+    unsigned long long *gh = hist + (long long)sg.pair * pitch + sg.kb;
+    unsigned my_oor = 0;
+    const int nunits = (tk.item_end - tk.item_begin) * kSub;
+    for (int u = warp; u < nunits; u += kHistThreads / 32) {
+      const int2 it = __ldg(&items[tk.item_begin + u / kSub]);
+      const int sub = u % kSub;
+      const bool diag = it.y < 0;
+      const int2 TI = __ldg(&tiles[it.x]);
+      const int2 TJ = __ldg(&tiles[it.y & 0x7fffffff]);
+      if (sub * 32 >= TI.y) continue;  // warp-uniform: empty sub-block
+      const int pi = sub * 32 + lane;
+      const bool active = pi < TI.y;
+      const float4 a = __ldg(&atoms[TI.x + (active ? pi : TI.y - 1)]);
+      // diag tile (same tile, same species): pairs j <= i incl. i == j,
+      // the reference's `dist` kernel (cuDebye-v15.cu:137).
+      const int jend_lane = active ? (diag ? pi + 1 : TJ.y) : 0;
+      const int jend = diag ? min(TJ.y, sub * 32 + 32) : TJ.y;
+      const float4 *bj = atoms + TJ.x;
+#pragma unroll 4
+      for (int j = 0; j < jend; ++j) {
+        const float4 b = __ldg(&bj[j]);  // warp-uniform address: broadcast
+        if (j < jend_lane) {
+          const int k = exact_bin(a.x, a.y, a.z, b, inv);
+          const unsigned lk = (unsigned)(k - sg.kb);
+          if (lk < (unsigned)sg.wl)
+            add16(sh, lk, gh);
+          else if ((unsigned)k >= nbins)
+            ++my_oor;
+        }
+      }
+    }
+    my_oor = __reduce_add_sync(0xffffffffu, my_oor);
+    if (lane == 0 && my_oor) atomicAdd(&s_oor, my_oor);
+    __syncthreads();
+    unsigned *dst = partial + (size_t)t * (size_t)words_per_task;
+    for (int i = threadIdx.x; i < nw; i += kHistThreads) dst[i] = sh[i];
+    if (threadIdx.x == 0 && s_oor)
+      atomicAdd(oor_total, (unsigned long long)s_oor);
+    __syncthreads();
+  }
+}
+
+// Sum the packed windows of each segment's tasks into the int64 histogram.
+// A segment owns its window's bins (windows of one pair do not overlap), so
+// the adds are plain read-modify-writes; the wrap corrections of the tile
+// kernel were made earlier on the same stream.
+__global__ void hist_reduce_kernel(const unsigned *__restrict__ partial,
+                                   int words_per_task,
+                                   const HistSeg *__restrict__ segs,
+                                   unsigned long long *__restrict__ hist,
+                                   long long pitch) {
+  const HistSeg sg = segs[blockIdx.y];
+  const int nw = (sg.wl + 1) >> 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw;
+       i += gridDim.x * blockDim.x) {
+    unsigned long long lo = 0, hi = 0;
+    for (int t = sg.task_begin; t < sg.task_end; ++t) {
+      const unsigned w = partial[(size_t)t * (size_t)words_per_task + i];
+      lo += w & 0xFFFFu;
+      hi += w >> 16;
+    }
+    unsigned long long *g = hist + (long long)sg.pair * pitch + sg.kb + 2 * i;
+    g[0] += lo;
+    g[1] += hi;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Planner (host).
+
+static void box_bins(const TileBox &A, const TileBox &B, double inv,
+                     int64_t *kmin, int64_t *kmax) {
+  double dmin2 = 0, dmax2 = 0;
+  for (int c = 0; c < 3; ++c) {
+    double g = std::max({0.0, (double)B.lo[c] - A.hi[c],
+                         (double)A.lo[c] - B.hi[c]});
+    double h = std::max(std::fabs((double)B.hi[c] - A.lo[c]),
+                        std::fabs((double)A.hi[c] - B.lo[c]));
+    dmin2 += g * g;
+    dmax2 += h * h;
+  }
+  // FP32 distances carry a relative error of a few 1e-7; widen generously.
+  *kmin = (int64_t)std::floor(std::sqrt(dmin2) * inv * (1 - 1e-5)) - 2;
+  *kmax = (int64_t)std::ceil(std::sqrt(dmax2) * inv * (1 + 1e-5)) + 2;
+}
+
+static int64_t item_pairs(int nI, int nJ, bool diag) {
+  return diag ? (int64_t)nI * (nI + 1) / 2 : (int64_t)nI * nJ;
+}
+
+Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
+                int64_t nbins, int target_tasks, HistPlan *plan) {
+  if (nbins < 1 || nbins > (int64_t(1) << 22))
+    return fail(DBX_ERR_ARG,
+                "histogram needs 1 <= nbins <= 4194304 (got " +
+                    std::to_string(nbins) + ")");
+  plan->items.clear();
+  plan->segs.clear();
+  plan->tasks.clear();
+  const int W = kWindowBins;
+  plan->window = (int)std::min<int64_t>(W, nbins);
+  const int64_t nwin = (nbins + W - 1) / W;
+  const double inv = 1.0 / rstep;
+  std::vector<std::vector<int2>> per_win(nwin);
+  std::vector<int64_t> seg_pairs;
+  std::vector<int2> seg_items;  // item range of each segment
+  plan->pairs = 0;
+  plan->nrows = (int)pairs.size();
+  for (size_t pi = 0; pi < pairs.size(); ++pi) {
+    const int a = pairs[pi].x, b = pairs[pi].y;
+    for (auto &v : per_win) v.clear();
+    for (int I = m.tile_start[a]; I < m.tile_start[a + 1]; ++I) {
+      const int J0 = (a == b) ? I : m.tile_start[b];
+      for (int J = J0; J < m.tile_start[b + 1]; ++J) {
+        const bool diag = (a == b) && (I == J);
+        const int2 it = make_int2(I, J | (diag ? int(0x80000000u) : 0));
+        if (nwin == 1) {
+          per_win[0].push_back(it);
+          continue;
+        }
+        int64_t kmin, kmax;
+        box_bins(m.boxes[I], m.boxes[J], inv, &kmin, &kmax);
+        int64_t w0 = std::max<int64_t>(0, kmin) / W;
+        int64_t w1 = std::min<int64_t>(std::max<int64_t>(kmax, 0), nbins - 1) / W;
+        w0 = std::min(w0, nwin - 1);  // entirely beyond rmax: still run it so
+        w1 = std::max(w1, w0);        // the kernel reports the range error
+        for (int64_t w = w0; w <= w1; ++w) per_win[w].push_back(it);
+      }
+    }
+    for (int64_t w = 0; w < nwin; ++w) {
+      if (per_win[w].empty()) continue;
+      HistSeg s;
+      s.pair = (int)pi;
+      s.kb = (int)(w * W);
+      s.wl = (int)std::min<int64_t>(W, nbins - w * W);
+      s.task_begin = s.task_end = 0;
+      int64_t sp = 0;
+      const int first = (int)plan->items.size();
+      for (const int2 &it : per_win[w]) {
+        const int2 TI = m.tiles[it.x], TJ = m.tiles[it.y & 0x7fffffff];
+        sp += item_pairs(TI.y, TJ.y, it.y < 0);
+        plan->items.push_back(it);
+      }
+      plan->segs.push_back(s);
+      seg_pairs.push_back(sp);
+      seg_items.push_back(make_int2(first, (int)plan->items.size()));
+    }
+    const int64_t na = m.sp_count[a], nb = m.sp_count[b];
+    plan->pairs += (a == b) ? na * (na + 1) / 2 : na * nb;
+  }
+  // Split segments into about target_tasks tasks of equal pair counts.
+  int64_t total = 0;
+  for (int64_t v : seg_pairs) total += v;
+  const int64_t target =
+      std::max<int64_t>(total / std::max(1, target_tasks), 1);
+  for (size_t s = 0; s < plan->segs.size(); ++s) {
+    HistSeg &sg = plan->segs[s];
+    sg.task_begin = (int)plan->tasks.size();
+    int64_t acc = 0;
+    int begin = seg_items[s].x;
+    for (int i = seg_items[s].x; i < seg_items[s].y; ++i) {
+      const int2 it = plan->items[i];
+      const int2 TI = m.tiles[it.x], TJ = m.tiles[it.y & 0x7fffffff];
+      acc += item_pairs(TI.y, TJ.y, it.y < 0);
+      if (acc >= target || i + 1 == seg_items[s].y) {
+        HistTask t;
+        t.seg = (int)s;
+        t.item_begin = begin;
+        t.item_end = i + 1;
+        t.pad = 0;
+        plan->tasks.push_back(t);
+        begin = i + 1;
+        acc = 0;
+      }
+    }
+    sg.task_end = (int)plan->tasks.size();
+  }
+  return ok();
+}
+
+static Error ensure(DevBuf *b, size_t bytes, size_t *delta) {
+  if (b->bytes >= bytes) return ok();
+  if (b->p) {
+    cudaFree(b->p);
+    *delta -= b->bytes;
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
+  b->bytes = bytes;
+  *delta += bytes;
+  return ok();
+}
+
+Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
+               int64_t nbins, int64_t pitch, unsigned long long *d_out,
+               HistWorkspace *ws, cudaStream_t stream, int num_sms,
+               size_t *ws_bytes_delta, Timers *tm) {
+  const int ntasks = (int)plan.tasks.size();
+  const int nsegs = (int)plan.segs.size();
+  int max_wl = 0;
+  for (const HistSeg &s : plan.segs) max_wl = std::max(max_wl, s.wl);
+  const int words = (max_wl + 1) / 2;
+  DBX_TRY(ensure(&ws->items, std::max<size_t>(plan.items.size(), 1) * sizeof(int2),
+                 ws_bytes_delta));
+  DBX_TRY(ensure(&ws->segs, std::max(nsegs, 1) * sizeof(HistSeg), ws_bytes_delta));
+  DBX_TRY(ensure(&ws->tasks, std::max(ntasks, 1) * sizeof(HistTask), ws_bytes_delta));
+  DBX_TRY(ensure(&ws->partial, std::max<size_t>((size_t)ntasks * words, 1) * 4,
+                 ws_bytes_delta));
+  DBX_TRY(ensure(&ws->oor, sizeof(unsigned long long), ws_bytes_delta));
+  DBX_CUDA_TRY(cudaMemsetAsync(
+      d_out, 0, sizeof(unsigned long long) * (size_t)pitch * plan.nrows, stream));
+  if (ntasks == 0) return ok();
+  DBX_CUDA_TRY(cudaMemcpyAsync(ws->items.p, plan.items.data(),
+                               plan.items.size() * sizeof(int2),
+                               cudaMemcpyHostToDevice, stream));
+  DBX_CUDA_TRY(cudaMemcpyAsync(ws->segs.p, plan.segs.data(),
+                               nsegs * sizeof(HistSeg), cudaMemcpyHostToDevice,
+                               stream));
+  DBX_CUDA_TRY(cudaMemcpyAsync(ws->tasks.p, plan.tasks.data(),
+                               ntasks * sizeof(HistTask),
+                               cudaMemcpyHostToDevice, stream));
+  DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, sizeof(unsigned long long), stream));
+  const int smem = words * 4;
+  DBX_CUDA_TRY(cudaFuncSetAttribute(hist_tiles_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kHistSmemBytes));
+  const int grid = std::min(ntasks, num_sms);
+  tm->start(DBX_T_HIST, stream);
+  hist_tiles_kernel<<<grid, kHistThreads, smem, stream>>>(
+      m.d_atoms, m.d_tiles, (const int2 *)ws->items.p,
+      (const HistTask *)ws->tasks.p, ntasks, (const HistSeg *)ws->segs.p,
+      inv_rstep, (unsigned)nbins, (unsigned *)ws->partial.p, words, d_out,
+      (long long)pitch, (unsigned long long *)ws->oor.p);
+  DBX_CUDA_TRY(cudaGetLastError());
+  tm->stop(DBX_T_HIST, stream);
+  tm->start(DBX_T_HIST_REDUCE, stream);
+  dim3 rgrid((words + 255) / 256, nsegs);
+  hist_reduce_kernel<<<rgrid, 256, 0, stream>>>((const unsigned *)ws->partial.p,
+                                                words,
+                                                (const HistSeg *)ws->segs.p,
+                                                d_out, (long long)pitch);
+  DBX_CUDA_TRY(cudaGetLastError());
+  tm->stop(DBX_T_HIST_REDUCE, stream);
+  unsigned long long oor = 0;
+  DBX_CUDA_TRY(cudaMemcpyAsync(&oor, ws->oor.p, sizeof(oor),
+                               cudaMemcpyDeviceToHost, stream));
+  DBX_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (oor)
+    return fail(DBX_ERR_RANGE,
+                std::to_string(oor) +
+                    " distances bin at or beyond rmax (nbins = " +
+                    std::to_string(nbins) + "); increase rmax");
+  return ok();
+}
+
+}  // namespace dbx

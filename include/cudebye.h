@@ -1,0 +1,184 @@
+/*
+ * cudebye.h — C ABI of the GB300 Debye scattering engine.
+ *
+ * Drop-in for the hot path of cuDebye v1.5 (cuDebye-v15.cu). The reference
+ * has no library interface: its path is the chain of host functions called
+ * from main() for every species pair (cuDebye-v15.cu:941-967). Each entry
+ * point below names the reference function it replaces. All entry points
+ * are plain C: pointers, sizes and status codes; no CUDA or C++ types.
+ *
+ * Conventions
+ *  - Every call returns DBX_OK (0) or a negative DBX_ERR_* code, and never
+ *    exits the process (the reference calls exit() in gpuErrchk,
+ *    cuDebye-v15.cu:58-66). dbx_last_error() gives the message of the last
+ *    failed call on a context.
+ *  - Host buffers belong to the caller; device memory belongs to the
+ *    context. Calls are synchronous: on return the results are in the
+ *    caller's host buffers.
+ *  - One context per host thread (a context is not thread-safe).
+ *  - Species pairs are numbered in the reference's loop order
+ *    (cuDebye-v15.cu:941-942): for row = 0..P-1, for col = row..P-1.
+ *    pair_index(row, col) = row*P - row*(row-1)/2 + (col - row).
+ */
+#ifndef CUDEBYE_H
+#define CUDEBYE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DBX_OK 0
+#define DBX_ERR_ARG (-1)      /* invalid argument */
+#define DBX_ERR_CUDA (-2)     /* CUDA runtime error */
+#define DBX_ERR_NOMEM (-3)    /* host or device allocation failed / HBM budget */
+#define DBX_ERR_FILE (-4)     /* input file missing (cuDebye-v15.cu:619-622) */
+#define DBX_ERR_PARSE (-5)    /* malformed .deb header or coordinate line */
+#define DBX_ERR_COUNT (-6)    /* atom count != header total (:830-833) */
+#define DBX_ERR_RANGE (-7)    /* a distance bins at or beyond rmax: the
+                                 reference writes out of bounds there
+                                 (README.md "Third Line") */
+#define DBX_ERR_MODEL (-8)    /* unknown model id */
+#define DBX_ERR_TIMEOUT (-9)  /* a bounded device-side wait ran out */
+#define DBX_ERR_IO (-10)      /* output file could not be written */
+
+typedef struct dbx_ctx dbx_ctx;
+
+/* One species ("subgroup") of a .deb file (cuDebye-v15.cu:786): occupancy,
+ * isotropic B (Beq) and the 11-parameter scattering factor
+ * f = c + sum_i a_i exp(-b_i K^2/16 pi^2). */
+typedef struct dbx_species {
+  double occ, beq;
+  double a[5], b[5], c;
+} dbx_species;
+
+/* Precision of the Debye sum. */
+#define DBX_DEBYE_TC 0   /* tensor-core split contraction, FP64 chunk
+                            reduction: max rel. error <= 1e-6 vs FP64 */
+#define DBX_DEBYE_FP64 1 /* FP64 CUDA-core direct sum (the reference's
+                            arithmetic, debyeRowSum cuDebye-v15.cu:493-538) */
+#define DBX_DEBYE_FP32 2 /* plain FP32 direct sum (unbatched FP32 form) */
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Create a context on `device` (the reference's .deb line 1 device,
+ * cudaSetDevice at cuDebye-v15.cu:646). hbm_budget_bytes = 0: no limit
+ * beyond the device's free memory. */
+int dbx_create(dbx_ctx **ctx, int device, size_t hbm_budget_bytes);
+int dbx_destroy(dbx_ctx *ctx);
+const char *dbx_strerror(int code);
+const char *dbx_last_error(const dbx_ctx *ctx);
+/* Bytes of device memory the context holds now. */
+size_t dbx_device_bytes(const dbx_ctx *ctx);
+
+/* ---- models ----------------------------------------------------------- */
+
+/* Upload one atomistic model: FP32 SoA coordinates grouped by species in
+ * species order (the reference's x/y/z arrays and start/end ranges,
+ * cuDebye-v15.cu:770-833 and :887-909). species_counts[i] atoms belong to
+ * species i. The model stays resident on the device until dbx_model_free
+ * or dbx_destroy; the engine keeps its own spatially sorted copy. */
+int dbx_model_upload(dbx_ctx *ctx, const float *x, const float *y,
+                     const float *z, const int64_t *species_counts,
+                     int nspecies, int64_t *model_id);
+int dbx_model_free(dbx_ctx *ctx, int64_t model_id);
+
+/* ---- hot path 1: distance histogram ----------------------------------- */
+
+/* Histogram of species pair (row, col), row <= col, into out_counts[nbins]
+ * (int64, host). Replaces splitCalcDist + its kernels dist / dist2 /
+ * care_dist2 (cuDebye-v15.cu:88-272): bin = (int)roundf(sqrtf((dx*dx +
+ * dy*dy) + dz*dz) * float(1/rstep)) in unfused FP32, the diagonal block
+ * counting i == j. Bit-exact with the reference. Returns DBX_ERR_RANGE if
+ * any pair bins at k >= nbins. nbins is normally int(rmax/rstep)+2
+ * (cuDebye-v15.cu:732; see dbx_channels). */
+int dbx_pair_histogram(dbx_ctx *ctx, int64_t model_id, int row, int col,
+                       double rstep, int64_t nbins, int64_t *out_counts);
+
+/* All P(P+1)/2 pair histograms in one device pass, out_counts
+ * [npairs][nbins] in pair order (the pair loop cuDebye-v15.cu:941-967). */
+int dbx_histogram(dbx_ctx *ctx, int64_t model_id, double rstep, int64_t nbins,
+                  int64_t *out_counts);
+
+/* int(rmax/rstep)+2 (cuDebye-v15.cu:732). */
+int64_t dbx_channels(double rmax, double rstep);
+
+/* Self-checks of reduceCheck (cuDebye-v15.cu:360-410) on one pair
+ * histogram: expected total n_a(n_a+1)/2 (diag) or n_a*n_b, bin 0 == n_a
+ * (diag), and the count of distances below 0.25 A beyond the self pairs
+ * ("possible atom collision"). Results in out[0..3] = {expected, observed,
+ * zero-distance count (r <= 0.0005, diag) , collisions}. Returns DBX_OK;
+ * the caller decides how to warn. */
+int dbx_reduce_check(const int64_t *counts, int64_t nbins, double rstep,
+                     int64_t n_row, int64_t n_col, int diag, int64_t out[4]);
+
+/* ---- hot path 2: Debye sum -------------------------------------------- */
+
+/* 2theta grid and K = 4 pi sin(theta)/lambda (cuDebye-v15.cu:690-698).
+ * Returns the number of points int((max-min)/step)+1; fills the arrays when
+ * they are non-NULL (they must hold that many doubles). */
+int dbx_k_grid(double lambda, double tt_min, double tt_max, double tt_step,
+               double *two_theta, double *K);
+
+/* Prefactor o_a o_b exp(-(B_a+B_b)K^2/16pi^2) f_a(K) f_b(K) of one pair on
+ * the device, FP64 (atomicProp/atomicScatter, cuDebye-v15.cu:447-479). */
+int dbx_atomic_prop(dbx_ctx *ctx, const dbx_species *a, const dbx_species *b,
+                    const double *K, int nq, double *out_ff);
+
+/* Intensity of one model: I[q] = sum over pairs of ff_pair(q) *
+ * sum_k m_k sin(K r_k)/(K r_k), r_k = k*rstep, m_k = 2 n_k (r_k > 0.0005),
+ * n_k otherwise (intensity/debyeRowSum, cuDebye-v15.cu:493-577, summed over
+ * the pair loop :941-967). Computes the histograms on the device first
+ * (they are kept resident for re-scoring with new K or species). mode is
+ * DBX_DEBYE_*. sp holds nspecies entries. out_I[nq] (host). */
+int dbx_intensity(dbx_ctx *ctx, int64_t model_id, double rstep, int64_t nbins,
+                  const dbx_species *sp, const double *K, int nq, int mode,
+                  double *out_I);
+
+/* One full pattern: recompute every pair histogram of the model (no cached
+ * histograms are used) and the Debye sum, as one pass of the reference's
+ * pair loop (cuDebye-v15.cu:941-967) does. Same arguments as
+ * dbx_intensity. */
+int dbx_pattern(dbx_ctx *ctx, int64_t model_id, double rstep, int64_t nbins,
+                const dbx_species *sp, const double *K, int nq, int mode,
+                double *out_I);
+
+/* ---- streams and timing ----------------------------------------------- */
+
+/* Launch on the caller's CUDA stream (a cudaStream_t passed as void*);
+ * NULL returns to the context's own stream. The reference has no
+ * counterpart (it runs on the legacy default stream). */
+int dbx_set_stream(dbx_ctx *ctx, void *cuda_stream);
+
+/* Device time of the phases of the last histogram / Debye call, measured
+ * with CUDA events on the launching stream when enabled (timing adds one
+ * event pair per launch). The reference printed clock() wall times
+ * (cuDebye-v15.cu:928-971). */
+#define DBX_T_HIST 0        /* tile-pair histogram kernel */
+#define DBX_T_HIST_REDUCE 1 /* merge of the CTA windows */
+#define DBX_T_PREFACTOR 2   /* atomicScatter equivalent */
+#define DBX_T_DEBYE 3       /* Debye sum kernels */
+#define DBX_NTIMERS 4
+int dbx_set_timing(dbx_ctx *ctx, int enable);
+int dbx_get_timing(const dbx_ctx *ctx, double out_ms[DBX_NTIMERS]);
+
+/* Host<->device bytes the context has copied since it was created:
+ * out[0] host to device, out[1] device to host. */
+int dbx_get_traffic(const dbx_ctx *ctx, int64_t out[2]);
+
+/* ---- whole-file drop-in ----------------------------------------------- */
+
+/* The reference's main() (cuDebye-v15.cu:599-1004) on the GPU: read
+ * `deb_path`, write <out_prefix>x<row>x<col> (hist 1/2) and <out_prefix>I
+ * (hist 0/2), byte-compatible with the reference's outputs on a POSIX host.
+ * out_prefix NULL = deb_path, as the reference does. verbose != 0 prints
+ * the reference-style progress log to stdout. */
+int dbx_run_deb(dbx_ctx *ctx, const char *deb_path, const char *out_prefix,
+                int verbose);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,135 @@
+"""GPU histogram parity: the engine's int64 pair histograms must equal the
+CPU oracle's bin for bin (the reference's FP32 formula, cuDebye-v15.cu:
+88-146), through the C ABI, on seeded inputs and the reference's edge
+cases: diagonal blocks with i == j, ragged tiles, one-atom species,
+windows split across shared-memory capacity, 16-bit counter wraps, and
+distances beyond rmax."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import cudebye_gb300 as cd
+from cudebye_gb300 import lattice
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_vs_oracle(engine, orc, xyz, counts, rstep, nbins):
+    m = engine.upload(xyz, counts)
+    try:
+        got = engine.histogram(m, rstep, nbins)
+    finally:
+        m.free()
+    want, bad = orc.model_histograms(xyz, counts, rstep, nbins)
+    assert bad == 0
+    np.testing.assert_array_equal(got, want)
+    return got
+
+
+@pytest.mark.parametrize("counts,seed", [
+    ([1], 0), ([2], 1), ([127], 2), ([128], 3), ([129], 4),
+    ([300, 1], 5), ([1, 1, 1], 6), ([513, 77, 250], 7), ([1000, 3000], 8)])
+def test_random_clusters(engine, orc, counts, seed):
+    rng = np.random.default_rng(seed)
+    n = sum(counts)
+    xyz = rng.uniform(-12, 12, size=(n, 3)).astype(np.float32)
+    nbins = cd.channels(45.0, 1e-3)
+    gpu_vs_oracle(engine, orc, xyz, counts, 1e-3, nbins)
+
+
+def test_plain_small_workload(engine, orc):
+    m = lattice.plain_small()
+    h = gpu_vs_oracle(engine, orc, m.xyz, m.counts, m.rstep, m.nbins)
+    assert int(h.sum()) == m.pairs
+
+
+def test_multi_window(engine, orc):
+    """Fine bins: 400,002 bins exceed one shared-memory window, so tile
+    pairs are grouped into several windows by their bounding boxes."""
+    m = lattice.spinel(radius=14.0, target=1500, seed=11, rstep=1e-4)
+    nbins = cd.channels(40.0, 1e-4)
+    gpu_vs_oracle(engine, orc, m.xyz, m.counts, 1e-4, nbins)
+
+
+def test_single_pair_entry_point(engine, orc):
+    m = lattice.spinel(radius=12.0, target=1200, seed=12)
+    mod = engine.upload(m.xyz, m.counts)
+    starts = np.concatenate([[0], np.cumsum(m.counts)[:-1]])
+    try:
+        for (r, c) in cd.pair_list(len(m.counts)):
+            got = engine.split_calc_dist(mod, r, c, m.rstep, m.nbins)
+            want, _ = orc.block_histogram(m.xyz, starts[r], m.counts[r],
+                                          starts[c], m.counts[c], r == c,
+                                          m.rstep, m.nbins)
+            np.testing.assert_array_equal(got, want)
+    finally:
+        mod.free()
+
+
+def test_exact_lattice_ties(engine, orc):
+    """Unjittered lattice: many exactly equal distances and x.5 bin ties."""
+    g = np.arange(12, dtype=np.float32) * np.float32(0.5)
+    xyz = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    gpu_vs_oracle(engine, orc, xyz, [len(xyz)], 0.25, cd.channels(12, 0.25))
+    gpu_vs_oracle(engine, orc, xyz, [900, len(xyz) - 900], 1e-3,
+                  cd.channels(12, 1e-3))
+
+
+def test_counter_wraps(orc, tmp_path):
+    """Millions of pairs in one bin per CTA task: the packed 16-bit shared
+    counters wrap many times (low half into high half and out of the word)
+    and must still give exact counts. Runs in a child process with few
+    tasks so each task sees >65535 counts in a bin."""
+    code = r"""
+import numpy as np, sys
+sys.path.insert(0, %r)
+import cudebye_gb300 as cd
+from oracle import pyoracle as orc
+n0, n1 = 7000, 5000
+xyz = np.zeros((n0 + n1 + 3, 3), np.float32)
+xyz[n0:n0 + n1, 0] = 1.0          # species 1 at x = 1: all 0-1 pairs in bin 1
+xyz[-3:] = [[0.5, 0, 0], [0, 0.5, 0], [0, 0, 3]]
+counts = [n0, n1, 3]
+with cd.Engine(0) as e:
+    m = e.upload(xyz, counts)
+    got = e.histogram(m, 1.0, 8)
+want, bad = orc.model_histograms(xyz, counts, 1.0, 8)
+assert bad == 0
+np.testing.assert_array_equal(got, want)
+assert got[0, 0] == n0 * (n0 + 1) // 2 and got[1, 1] == n0 * n1
+print("OK")
+""" % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, DBX_HIST_TASKS="3")
+    r = subprocess.run(["python", "-c", code], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
+def test_out_of_range_is_an_error(engine):
+    """A distance beyond rmax: the reference writes out of bounds
+    (README.md, "Third Line"); the engine returns DBX_ERR_RANGE."""
+    xyz = np.array([[0, 0, 0], [0, 0, 10]], np.float32)
+    m = engine.upload(xyz, [2])
+    try:
+        with pytest.raises(cd.DebyeError) as e:
+            engine.histogram(m, 0.1, cd.channels(5.0, 0.1))
+        assert e.value.code == -7
+        h = engine.histogram(m, 0.1, cd.channels(10.0, 0.1))  # context still usable
+        assert h[0, 0] == 2 and h[0, 100] == 1
+    finally:
+        m.free()
+
+
+def test_bad_arguments(engine):
+    m = engine.upload(np.zeros((2, 3), np.float32), [2])
+    try:
+        with pytest.raises(cd.DebyeError) as e:
+            engine.split_calc_dist(m, 1, 0, 0.1, 10)
+        assert e.value.code == -1
+    finally:
+        m.free()
+    with pytest.raises(cd.DebyeError) as e:
+        engine.histogram(m, 0.1, 10)
+    assert e.value.code == -8

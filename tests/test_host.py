@@ -1,0 +1,181 @@
+"""CPU tests: host logic, file formats, the C-ABI library's exports, and a
+bit-level model of the device histogram's arithmetic. No GPU needed."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cudebye_gb300 as cd
+from cudebye_gb300 import lattice
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "cudebye.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(dbx_\w+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from cudebye_gb300 import build
+    return build.build()
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = ctypes.CDLL(built_lib)  # loads without a GPU
+    syms = declared_symbols()
+    assert syms, "no declarations parsed"
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(syms) == set(cd.EXPORTS), "python binding list out of date"
+
+
+def test_host_entry_points_without_gpu(built_lib):
+    """The pure host entry points run without a device."""
+    lib = cd.load_library(built_lib)
+    assert lib.dbx_channels(356.0, 0.0001) == int(356 / 0.0001) + 2
+    n = lib.dbx_k_grid(1.5418, 10.0, 140.0, 0.02, None, None)
+    assert n == 6501
+    tt = np.zeros(n)
+    K = np.zeros(n)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.dbx_k_grid(1.5418, 10.0, 140.0, 0.02, tt.ctypes.data_as(dp),
+                   K.ctypes.data_as(dp))
+    tt2, K2 = cd.k_grid(1.5418, 10.0, 140.0, 0.02)
+    np.testing.assert_array_equal(tt, tt2)
+    np.testing.assert_allclose(K, K2, rtol=1e-15)
+    assert lib.dbx_strerror(-7) == b"distance beyond rmax"
+    # no device: creating a context fails cleanly, with a status, no exit
+    ctx = ctypes.c_void_p()
+    rc = lib.dbx_create(ctypes.byref(ctx), 0, 0)
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        assert rc == -2 and not ctx
+
+
+def test_k_grid_matches_oracle(orc):
+    for grid in [(1.5418, 10.0, 140.0, 0.02), (1.5406, 10.0, 130.0, 0.02),
+                 (0.7107, 5.0, 150.0, 145.0 / 19999)]:
+        tt, K = cd.k_grid(*grid)
+        tt2, K2 = orc.k_grid(*grid)
+        assert len(tt) == len(tt2)
+        np.testing.assert_array_equal(tt, tt2)
+        np.testing.assert_allclose(K, K2, rtol=1e-15)
+
+
+def test_channels():
+    assert cd.channels(356, 0.0001) == 3560002  # Data/cmd-logfile.txt
+    assert cd.channels(122, 0.0001) == int(122 / 0.0001) + 2
+
+
+def test_reduce_check():
+    h = np.zeros(100, np.int64)
+    h[0] = 10
+    h[30] = 45
+    r = cd.reduce_check(h, 0.1, 10, 10, True)
+    assert r["expected"] == 55 and r["observed"] == 55 and r["bin0"] == 10
+    assert r["collisions"] == 0
+    h[1] = 2  # two pairs at 0.1 A: below the 0.25 A "collision" limit
+    r = cd.reduce_check(h, 0.1, 10, 10, True)
+    assert r["collisions"] == 2
+
+
+def test_read_deb_fixture(golden_deb):
+    d = cd.read_deb(golden_deb["UH3"])
+    assert d.counts == [27972, 8931] and d.names == ["H", "U"]
+    assert d.hist == 0 and d.rmax == 122 and d.rstep == 0.0001
+    assert d.xyz.shape == (36903, 3) and d.xyz.dtype == np.float32
+    assert d.xyz[0].tolist() == [np.float32(-33.215), np.float32(-32.18533),
+                                 np.float32(-31.20217)]
+    assert abs(d.species[1].a[0] - 15.679275) < 1e-12
+
+
+def test_read_deb_errors(tmp_path):
+    with pytest.raises(cd.DebyeError) as e:
+        cd.read_deb(str(tmp_path / "missing.deb"))
+    assert e.value.code == -4
+    p = tmp_path / "bad.deb"
+    p.write_text("0 8 1024\n1.5 10 20 0.1\n10 0.01 0\n1\n"
+                 "2 O 1 0 1 1 1 1 1 1 1 1 1 1 0\n0 0 0\n")
+    with pytest.raises(cd.DebyeError) as e:
+        cd.read_deb(str(p))
+    assert e.value.code == -6
+
+
+def test_synthetic_workloads():
+    m = lattice.plain_small()
+    assert m.natoms == 5000 and m.counts == [2000, 3000]
+    assert m.pairs == 12502500  # 5000*5001/2
+    tt, K = m.k_grid()
+    assert len(tt) == 6001
+    m2 = lattice.plain_small()
+    np.testing.assert_array_equal(m.xyz, m2.xyz)  # seeded
+    s = lattice.spinel_10nm()
+    assert abs(s.natoms - 118000) < 300 and len(s.counts) == 3
+    assert 100000 <= s.nbins <= 110000
+    p = lattice.precision()
+    assert len(p.k_grid()[0]) == 20000
+
+
+def test_xyz2deb_rmax_rule():
+    xyz = np.array([[0, 0, 0], [10, 0, 0]], np.float32)
+    # centred half-extent 5 -> 2*ceil(5*1.025) = 12 (Matlab/xyz2deb.m:204)
+    assert lattice.xyz2deb_rmax(xyz) == 12
+
+
+def _exact_bin_model(p):
+    """numpy model of the kernel's roundf: t = p + 2^23 (RN even), bits,
+    tie correction; must equal roundf (half away from zero) for p >= 0."""
+    p = np.asarray(p, np.float32)
+    t = (p + np.float32(8388608.0)).astype(np.float32)
+    k = t.view(np.int32).astype(np.int64) - 0x4B000000
+    r = (t - np.float32(8388608.0)).astype(np.float32)
+    k += ((p - r).astype(np.float32) == np.float32(0.5))
+    return k
+
+
+def test_exact_roundf_without_conversion():
+    rng = np.random.default_rng(0)
+    p = np.concatenate([
+        rng.uniform(0, 4.2e6, 200000).astype(np.float32),
+        (np.arange(0, 100000, dtype=np.float32) + np.float32(0.5)),  # ties
+        np.nextafter(np.float32(0.5), np.float32(0)).reshape(1),
+        np.array([0, 0.5, 1.5, 2.5, 4194303.5], np.float32)])
+    want = np.floor(p.astype(np.float64) + 0.5).astype(np.int64)  # p exact in f64
+    np.testing.assert_array_equal(_exact_bin_model(p), want)
+
+
+def test_packed_counter_bookkeeping():
+    """Serial model of add16: two 16-bit bins per 32-bit word, wraps and the
+    low->high carry compensated in an int64 side array; true counts are
+    recovered exactly for adversarial orders."""
+    rng = np.random.default_rng(1)
+    for trial in range(20):
+        nadd = 300000
+        bins = rng.choice(2, size=nadd, p=[0.5, 0.5])
+        if trial % 3 == 0:
+            bins[:] = 0
+        if trial % 3 == 1:
+            bins[:] = 1
+        word = 0
+        glob = [0, 0, 0]
+        for b in bins:
+            sh = 16 * b
+            old = word
+            word = (word + (1 << sh)) & 0xFFFFFFFF
+            if ((old >> sh) & 0xFFFF) == 0xFFFF:
+                glob[b] += 65536
+                if sh == 0:
+                    glob[1] -= 1
+                    if (old >> 16) == 0xFFFF:
+                        glob[1] += 65536
+        got = [(word & 0xFFFF) + glob[0], (word >> 16) + glob[1]]
+        assert got == [int((bins == 0).sum()), int((bins == 1).sum())]
