@@ -124,6 +124,7 @@ def test_out_of_range_is_an_error(engine):
 
 def test_bad_arguments(engine):
     m = engine.upload(np.zeros((2, 3), np.float32), [2])
+    stale = cd.Model(engine, m.id, m.counts)
     try:
         with pytest.raises(cd.DebyeError) as e:
             engine.split_calc_dist(m, 1, 0, 0.1, 10)
@@ -131,5 +132,5 @@ def test_bad_arguments(engine):
     finally:
         m.free()
     with pytest.raises(cd.DebyeError) as e:
-        engine.histogram(m, 0.1, 10)
+        engine.histogram(stale, 0.1, 10)
     assert e.value.code == -8
