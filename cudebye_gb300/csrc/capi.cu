@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "debio.h"
+#include "debye_tc.h"
 #include "engine.h"
 
 using dbx::Error;
@@ -30,6 +31,7 @@ struct dbx_ctx {
   std::map<int64_t, std::unique_ptr<dbx::Model>> models;
   int64_t next_id = 1;
   dbx::HistWorkspace hws;
+  dbx::TcState tc;
   dbx::DevBuf tmp_hist, K, ff, I;
   std::string last_error;
 };
@@ -156,14 +158,30 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   DBX_TRY(dbx::debye_prefactor(sp, m->nspecies, (const double *)c->K.p, nq,
                                (double *)c->ff.p, c->stream));
   c->tm.stop(DBX_T_PREFACTOR, c->stream);
-  // The tensor-core form is not built yet: DBX_DEBYE_TC runs the FP64 form.
-  const int kmode = mode == DBX_DEBYE_FP32 ? DBX_DEBYE_FP32 : DBX_DEBYE_FP64;
-  c->tm.start(DBX_T_DEBYE, c->stream);
-  DBX_TRY(dbx::debye_direct(kmode, m->d_hist, np, m->hist_pitch, nbins, rstep,
-                            (const double *)c->K.p, nq,
-                            (const double *)c->ff.p, (double *)c->I.p,
-                            c->stream));
-  c->tm.stop(DBX_T_DEBYE, c->stream);
+  if (mode == DBX_DEBYE_TC) {
+    std::vector<dbx::TcCol> cols(np);
+    for (int p = 0; p < np; ++p) {
+      cols[p].hist = m->d_hist + (size_t)p * m->hist_pitch;
+      cols[p].nbins = nbins;
+      cols[p].ff = (const double *)c->ff.p + (size_t)p * nq;
+    }
+    size_t delta = 0;
+    const int64_t h0 = c->tc.h2d, d0 = c->tc.d2h;
+    Error e = dbx::debye_tc(&c->tc, cols, {0, np}, rstep, K,
+                            (const double *)c->K.p, nq, (double *)c->I.p,
+                            c->stream, &delta, &c->tm);
+    c->used += delta;
+    c->h2d += c->tc.h2d - h0;
+    c->d2h += c->tc.d2h - d0;
+    if (e.code) return e;
+  } else {
+    c->tm.start(DBX_T_DEBYE, c->stream);
+    DBX_TRY(dbx::debye_direct(mode, m->d_hist, np, m->hist_pitch, nbins, rstep,
+                              (const double *)c->K.p, nq,
+                              (const double *)c->ff.p, (double *)c->I.p,
+                              c->stream));
+    c->tm.stop(DBX_T_DEBYE, c->stream);
+  }
   DBX_CUDA_TRY(cudaMemcpyAsync(out_I, c->I.p, sizeof(double) * nq,
                                cudaMemcpyDeviceToHost, c->stream));
   c->d2h += sizeof(double) * nq;
@@ -237,6 +255,7 @@ int dbx_destroy(dbx_ctx *c) {
   release(c, &c->hws.tasks);
   release(c, &c->hws.partial);
   release(c, &c->hws.oor);
+  dbx::tc_release(&c->tc);
   release(c, &c->tmp_hist);
   release(c, &c->K);
   release(c, &c->ff);

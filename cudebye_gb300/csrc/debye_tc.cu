@@ -1,0 +1,547 @@
+// debye_tc.cu — tensor-core Debye contraction on sm_103a (tcgen05 + TMEM).
+//
+// The reference sums, per species pair and per q (debyeRowSum,
+// cuDebye-v15.cu:493-538),
+//     S(q) = sum_k m_k sin(q r_k)/(q r_k),   r_k = k*rstep,
+// with m_k = 2 n_k off the self distance (r_k > 0.0005) and n_k on it.
+// Here the non-self part is rewritten as q*S'(q) = sum_k w_k sin(q r_k) with
+// w_k = m_k / r_k, and the bins are cut into chunks of L = 256:
+// k = k0 + j, k0 = ch*L, so sin(q r_k) = sin(q k0 dr) cos(q j dr)
+//                                       + cos(q k0 dr) sin(q j dr).
+// The j-basis [cos(q j dr) | sin(q j dr)] is the same for every chunk, so
+// the sum becomes one real GEMM
+//     D[row, n] = sum_j Basis[row, j] * W[n, j],   n = (pair, chunk)
+// (rows: Qp cosine rows then Qp sine rows), followed by an epilogue that
+// rotates each chunk by its twiddle (sin(q k0 dr) for cosine rows,
+// cos(q k0 dr) for sine rows) and sums the chunks of a pair.
+//
+// Precision (<= 1e-6 relative on the intensity vs FP64): both operands are
+// fixed-point integers split into four balanced base-256 digits, exact in
+// bf16 (|digit| <= 128). Digit products are exact integers and a K = 256
+// dot product of up to four digit pairs stays within 2^24, so the FP32
+// tensor-core accumulation is error-free. The digit pairs with s + t <= 3
+// (10 of 16) are accumulated into four TMEM accumulators by weight class;
+// the epilogue recombines them exactly into a double-float, applies the
+// per-chunk scale, the twiddle (double-float) and the chunk sum, and the
+// pair and q sums run in FP64.
+//
+// Kernel shape: CTA tile 128 rows x 64 columns, K = 256 in four slabs of
+// 64; operands are stored pre-tiled in global memory in the canonical
+// no-swizzle K-major core-matrix layout, so each slab is two contiguous
+// bulk copies (TMA engine, cp.async.bulk) completing on an mbarrier; one
+// thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> f32, M=128, N=64,
+// K=16) and commits to a second mbarrier; TMEM holds 4 x 64 f32 columns.
+// Every wait is bounded and reports a timeout through an error word.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "debye_tc.h"
+
+namespace dbx {
+namespace tc {
+
+constexpr int kL = 256;             // bins per chunk = GEMM K
+constexpr int kKS = 64;             // K per shared-memory slab
+constexpr int kNSlab = kL / kKS;    // 4
+constexpr int kTM = 128;            // rows per tile
+constexpr int kTN = 64;             // columns (chunks) per tile
+constexpr int kND = 4;              // digits per operand
+constexpr int kABlock = kTM * kKS;  // elements per digit per slab (16 KB)
+constexpr int kBBlock = kTN * kKS;  // 8 KB
+constexpr int kASlabBytes = kND * kABlock * 2;  // 64 KB
+constexpr int kBSlabBytes = kND * kBBlock * 2;  // 32 KB
+constexpr int kThreads = 128;
+constexpr int kTmemCols = 256;      // 4 classes x 64 columns
+constexpr int kSmemBytes = kASlabBytes + kBSlabBytes + 1024 + 64;
+constexpr double kSelfR = 0.0005;   // cuDebye-v15.cu:508
+
+// Element offset of (row, k) inside a [rows x 64] block stored as 8x8
+// core matrices (8 rows x 16 bytes each, contiguous), row groups outermost:
+// core (g, kc) at (g*8 + kc)*64 elements. Leading (K) byte offset 128,
+// stride (row-group) byte offset 1024.
+__host__ __device__ inline int tiled_off(int row, int k) {
+  return ((((row >> 3) << 3) + (k >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
+}
+
+// Balanced base-256 digits of v, |v| <= 2^31 - 1, most significant first:
+// v = d0*2^24 + d1*2^16 + d2*2^8 + d3, |d| <= 128.
+__device__ inline void split4(long long v, float d[4]) {
+  const int d3 = (int)(((v + 128) & 255) - 128);
+  v = (v - d3) >> 8;
+  const int d2 = (int)(((v + 128) & 255) - 128);
+  v = (v - d2) >> 8;
+  const int d1 = (int)(((v + 128) & 255) - 128);
+  v = (v - d1) >> 8;
+  d[0] = (float)v;
+  d[1] = (float)d1;
+  d[2] = (float)d2;
+  d[3] = (float)d3;
+}
+
+__device__ inline long long fixed31(double v) {
+  long long r = llrint(v * 2147483648.0);
+  return r > 2147483647LL ? 2147483647LL : (r < -2147483647LL ? -2147483647LL : r);
+}
+
+// Basis digits: rows [0,Qp) cos(K_q j dr), rows [Qp,2Qp) sin(K_q j dr).
+// Layout: [row tile][slab][digit][tiled 128 x 64].
+__global__ void basis_kernel(const double *__restrict__ K, int nq, int Qp,
+                             double rstep, __nv_bfloat16 *__restrict__ A) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 2LL * Qp * kL) return;
+  const int j = (int)(idx % kL);
+  const int m = (int)(idx / kL);
+  const bool sinrow = m >= Qp;
+  const int q = sinrow ? m - Qp : m;
+  double v = 0.0;
+  if (q < nq) {
+    const double ph = K[q] * ((double)j * rstep);
+    v = sinrow ? sin(ph) : cos(ph);
+  }
+  float d[4];
+  split4(fixed31(v), d);
+  const int mt = m / kTM, row = m % kTM, ks = j / kKS, k = j % kKS;
+  const size_t base = (size_t)(mt * kNSlab + ks) * kND * kABlock;
+#pragma unroll
+  for (int s = 0; s < kND; ++s)
+    A[base + (size_t)s * kABlock + tiled_off(row, k)] = __float2bfloat16_rn(d[s]);
+}
+
+// Twiddles per (chunk, q): alpha = K_q * ch*L*dr; (sin hi, sin lo, cos hi,
+// cos lo) as double-floats.
+__global__ void twiddle_kernel(const double *__restrict__ K, int nq, int Qp,
+                               int nch, double rstep, float4 *__restrict__ tw) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nch * Qp) return;
+  const int q = (int)(idx % Qp);
+  const int ch = (int)(idx / Qp);
+  double s = 0.0, c = 1.0;
+  if (q < nq) sincos(K[q] * ((double)ch * kL * rstep), &s, &c);
+  const float sh = (float)s, ch_ = (float)c;
+  tw[idx] = make_float4(sh, (float)(s - (double)sh), ch_, (float)(c - (double)ch_));
+}
+
+// Chunk weights w = m/r as digits, one warp per (tile, column).
+// Layout of W: [col tile][slab][digit][tiled 64 x 64]; E: per column,
+// the chunk's scale exponent (max|w| < 2^E).
+__global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
+                               const TcCol *__restrict__ cols, double rstep,
+                               __nv_bfloat16 *__restrict__ W,
+                               int *__restrict__ E,
+                               int *__restrict__ nonself) {
+  const int gw = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  const int nt = gw / kTN, n = gw % kTN;
+  if (nt >= ntiles) return;
+  const TcTile t = tiles[nt];
+  const TcCol col = cols[t.col];
+  const int ch = t.ch0 + n;
+  double w[8];
+  double mx = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const long long k = (long long)ch * kL + lane * 8 + i;
+    double v = 0.0;
+    if (k < col.nbins) {
+      const double cnt = (double)col.hist[k];
+      const double r = (double)k * rstep;  // r_reduced (cuDebye-v15.cu:735)
+      if (r > kSelfR && cnt != 0.0) v = (2.0 * cnt) / r;
+    }
+    w[i] = v;
+    mx = fmax(mx, fabs(v));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);  // mx < 2^e
+  const double scale = ldexp(1.0, 31 - e);
+  const int j0 = lane * 8, ks = j0 / kKS, k0 = j0 % kKS;
+  const size_t base = (size_t)(nt * kNSlab + ks) * kND * kBBlock + tiled_off(n, k0);
+  alignas(16) __nv_bfloat16 dig[kND][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    float d[4];
+    split4(fixed31(w[i] * scale), d);
+#pragma unroll
+    for (int s = 0; s < kND; ++s) dig[s][i] = __float2bfloat16_rn(d[s]);
+  }
+#pragma unroll
+  for (int s = 0; s < kND; ++s)
+    *reinterpret_cast<uint4 *>(W + base + (size_t)s * kBBlock) =
+        *reinterpret_cast<const uint4 *>(dig[s]);
+  if (lane == 0) {
+    E[nt * kTN + n] = e;
+    if (mx > 0.0) atomicOr(&nonself[t.col], 1);
+  }
+}
+
+// ---- PTX helpers ------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  // Bounded wait: ~2^22 polls (seconds at most), then report a timeout.
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo,
+                                              uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  return d;                // base offset 0, no swizzle
+}
+
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t ad,
+                                         uint64_t bd, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,"
+      "%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
+        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__global__ void __launch_bounds__(kThreads, 2)
+    gemm_kernel(const __nv_bfloat16 *__restrict__ A,
+                const __nv_bfloat16 *__restrict__ W,
+                const TcTile *__restrict__ tiles, const int *__restrict__ Ecol,
+                const float4 *__restrict__ tw, int Qp, int nrt,
+                double *__restrict__ P, int *__restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t *sbase = smem_raw + (base - raw);
+  const uint32_t sA = base, sB = base + kASlabBytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sbase + kASlabBytes + kBSlabBytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+  __shared__ int s_E[kTN];
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x % nrt, nt = blockIdx.x / nrt;
+  const uint32_t bar_load = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_load));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_mma));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    s_fail = 0;
+  }
+  if (tid < kTN) s_E[tid] = Ecol[nt * kTN + tid];
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+            smem_u32(tslot)),
+        "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tslot;
+
+  if (tid == 0) {
+    constexpr uint32_t idesc = make_idesc(kTM, kTN);
+    const char *gA = reinterpret_cast<const char *>(A) +
+                     (size_t)mt * kNSlab * kASlabBytes;
+    const char *gW = reinterpret_cast<const char *>(W) +
+                     (size_t)nt * kNSlab * kBSlabBytes;
+    bool ok = true;
+    for (int ks = 0; ks < kNSlab && ok; ++ks) {
+      asm volatile(
+          "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_load),
+          "r"(kASlabBytes + kBSlabBytes)
+          : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+          "[%0], [%1], %2, [%3];" ::"r"(sA),
+          "l"(gA + (size_t)ks * kASlabBytes), "r"(kASlabBytes), "r"(bar_load)
+          : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+          "[%0], [%1], %2, [%3];" ::"r"(sB),
+          "l"(gW + (size_t)ks * kBSlabBytes), "r"(kBSlabBytes), "r"(bar_load)
+          : "memory");
+      if (!mbar_wait(bar_load, ks & 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+#pragma unroll
+        for (int s = 0; s <= w; ++s) {
+          const int t = w - s;
+#pragma unroll
+          for (int kk = 0; kk < kKS / 16; ++kk) {
+            const uint64_t ad = make_desc(sA + s * kABlock * 2 + kk * 256, 128, 1024);
+            const uint64_t bd = make_desc(sB + t * kBBlock * 2 + kk * 256, 128, 1024);
+            const uint32_t acc = (ks > 0 || s > 0 || kk > 0) ? 1u : 0u;
+            mma_bf16(tmem + w * kTN, ad, bd, idesc, acc);
+          }
+        }
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
+          "[%0];" ::"r"(bar_mma)
+          : "memory");
+      if (!mbar_wait(bar_mma, ks & 1)) ok = false;
+    }
+    if (!ok) {
+      s_fail = 1;
+      atomicExch(err, 1);
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+
+  if (!s_fail) {
+    // Epilogue: row = TMEM lane; sum the 64 chunks of this tile.
+    const TcTile tile = tiles[nt];
+    const int row = warp * 32 + lane;
+    const int m = mt * kTM + row;
+    const bool sinrow = m >= Qp;
+    const int q = sinrow ? m - Qp : m;
+    const float4 *twq = tw + q;
+    float sh = 0.f, sl = 0.f;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int cg = 0; cg < kTN / 16; ++cg) {
+      uint32_t a0[16], a1[16], a2[16], a3[16];
+      tmem_ld16(lane_base + 0 * kTN + cg * 16, a0);
+      tmem_ld16(lane_base + 1 * kTN + cg * 16, a1);
+      tmem_ld16(lane_base + 2 * kTN + cg * 16, a2);
+      tmem_ld16(lane_base + 3 * kTN + cg * 16, a3);
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int n = cg * 16 + i;
+        const float hi = __uint_as_float(a0[i]);
+        const float lo = fmaf(__uint_as_float(a1[i]), 0x1p-8f,
+                              fmaf(__uint_as_float(a2[i]), 0x1p-16f,
+                                   __uint_as_float(a3[i]) * 0x1p-24f));
+        const float4 t = twq[(size_t)(tile.ch0 + n) * Qp];
+        const float th = sinrow ? t.z : t.x;
+        const float tl = sinrow ? t.w : t.y;
+        // (th + tl) * (hi + lo) as a double-float, scaled by 2^(E-14)
+        float p = th * hi;
+        float pe = fmaf(th, hi, -p);
+        pe = fmaf(th, lo, fmaf(tl, hi, pe));
+        const float sc = __int_as_float((s_E[n] - 14 + 127) << 23);
+        p *= sc;
+        pe *= sc;
+        const float s = sh + p;
+        const float bb = s - sh;
+        const float e2 = (sh - (s - bb)) + (p - bb);
+        sl += e2 + pe;
+        sh = s + sl;
+        sl = sl - (sh - s);
+      }
+    }
+    P[(size_t)nt * (2 * Qp) + m] = (double)sh + (double)sl;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile(
+        "tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+        "r"(kTmemCols));
+}
+
+// I[model][q] = sum over the model's columns (pair order) of
+// ff[q] * (self + (sum of the column's tiles of P over both row halves)/K).
+__global__ void reduce_kernel(const TcCol *__restrict__ cols, int ncols,
+                              const int *__restrict__ model_col_begin,
+                              int nmodels, const double *__restrict__ P,
+                              const int *__restrict__ nonself,
+                              const double *__restrict__ K, int nq, int Qp,
+                              double *__restrict__ I) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int mod = blockIdx.y;
+  if (q >= nq || mod >= nmodels) return;
+  const double Kq = K[q];
+  double acc = 0.0;
+  for (int c = model_col_begin[mod]; c < model_col_begin[mod + 1]; ++c) {
+    const TcCol col = cols[c];
+    double t = 0.0;
+    for (int nt = col.tile_begin; nt < col.tile_end; ++nt)
+      t += P[(size_t)nt * (2 * Qp) + q] + P[(size_t)nt * (2 * Qp) + Qp + q];
+    double S;
+    if (Kq == 0.0)  // sin(0)/0 of the reference (cuDebye-v15.cu:509)
+      S = nonself[c] ? __longlong_as_double(0x7ff8000000000000LL) : col.self;
+    else
+      S = col.self + t / Kq;
+    acc += S * col.ff[q];
+  }
+  I[(size_t)mod * nq + q] = acc;
+}
+
+// Self-distance sum of each column: bins with r <= 0.0005 (m = n there).
+__global__ void self_kernel(TcCol *cols, int ncols, double rstep) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  double s = 0.0;
+  for (long long k = 0; k < cols[c].nbins && (double)k * rstep <= kSelfR; ++k)
+    s += (double)cols[c].hist[k];
+  cols[c].self = s;
+}
+
+}  // namespace tc
+
+using namespace tc;
+
+static Error grow(DevBuf *b, size_t bytes, size_t *delta) {
+  if (b->bytes >= bytes) return ok();
+  if (b->p) {
+    cudaFree(b->p);
+    *delta -= b->bytes;
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
+  b->bytes = bytes;
+  *delta += bytes;
+  return ok();
+}
+
+void tc_release(TcState *st) {
+  for (DevBuf *b : {&st->basis, &st->twid, &st->W, &st->E, &st->P, &st->tiles,
+                    &st->cols, &st->mcb, &st->nonself, &st->err})
+    if (b->p) {
+      cudaFree(b->p);
+      b->p = nullptr;
+      b->bytes = 0;
+    }
+  st->grid_K.clear();
+}
+
+size_t tc_bytes(const TcState *st) {
+  size_t s = 0;
+  for (const DevBuf *b : {&st->basis, &st->twid, &st->W, &st->E, &st->P,
+                          &st->tiles, &st->cols, &st->mcb, &st->nonself, &st->err})
+    s += b->bytes;
+  return s;
+}
+
+Error debye_tc(TcState *st, std::vector<TcCol> cols,
+               const std::vector<int> &model_col_begin, double rstep,
+               const double *h_K, const double *d_K, int nq, double *d_I,
+               cudaStream_t stream, size_t *delta, Timers *tm) {
+  const int ncols = (int)cols.size();
+  const int nmodels = (int)model_col_begin.size() - 1;
+  if (ncols == 0 || nq < 1) return fail(DBX_ERR_ARG, "empty Debye contraction");
+  const int Qp = (nq + kTM - 1) / kTM * kTM;
+  const int nrt = 2 * Qp / kTM;
+  // Column tiles: each column (pair) gets ceil(nch/64) tiles of 64 chunks.
+  std::vector<TcTile> tiles;
+  int nch_max = 1;
+  for (int c = 0; c < ncols; ++c) {
+    const int nch = (int)((cols[c].nbins + kL - 1) / kL);
+    nch_max = std::max(nch_max, nch);
+    cols[c].tile_begin = (int)tiles.size();
+    for (int ch0 = 0; ch0 < std::max(nch, 1); ch0 += kTN) tiles.push_back({c, ch0, 0, 0});
+    cols[c].tile_end = (int)tiles.size();
+  }
+  const int nch_cap = (nch_max + kTN - 1) / kTN * kTN;  // twiddle rows
+  const int ntiles = (int)tiles.size();
+  // Plan data cached per (q grid, rstep, chunk count): basis and twiddles.
+  const bool same_grid = st->grid_K.size() == (size_t)nq && st->grid_rstep == rstep &&
+                         st->grid_nch >= nch_cap &&
+                         std::memcmp(st->grid_K.data(), h_K, sizeof(double) * nq) == 0;
+  DBX_TRY(grow(&st->W, (size_t)ntiles * kNSlab * kBSlabBytes, delta));
+  DBX_TRY(grow(&st->E, sizeof(int) * ntiles * kTN, delta));
+  DBX_TRY(grow(&st->P, sizeof(double) * ntiles * 2 * Qp, delta));
+  DBX_TRY(grow(&st->tiles, sizeof(TcTile) * ntiles, delta));
+  DBX_TRY(grow(&st->cols, sizeof(TcCol) * ncols, delta));
+  DBX_TRY(grow(&st->mcb, sizeof(int) * (nmodels + 1), delta));
+  DBX_TRY(grow(&st->nonself, sizeof(int) * ncols, delta));
+  DBX_TRY(grow(&st->err, sizeof(int), delta));
+  if (!same_grid) {
+    DBX_TRY(grow(&st->basis, (size_t)nrt * kNSlab * kASlabBytes, delta));
+    DBX_TRY(grow(&st->twid, sizeof(float4) * (size_t)nch_cap * Qp, delta));
+    const long long nb = 2LL * Qp * kL;
+    basis_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, stream>>>(
+        d_K, nq, Qp, rstep, (__nv_bfloat16 *)st->basis.p);
+    const long long nt2 = (long long)nch_cap * Qp;
+    twiddle_kernel<<<(unsigned)((nt2 + 255) / 256), 256, 0, stream>>>(
+        d_K, nq, Qp, nch_cap, rstep, (float4 *)st->twid.p);
+    DBX_CUDA_TRY(cudaGetLastError());
+    st->grid_K.assign(h_K, h_K + nq);
+    st->grid_rstep = rstep;
+    st->grid_nch = nch_cap;
+  }
+  DBX_CUDA_TRY(cudaMemcpyAsync(st->tiles.p, tiles.data(), sizeof(TcTile) * ntiles,
+                               cudaMemcpyHostToDevice, stream));
+  DBX_CUDA_TRY(cudaMemcpyAsync(st->cols.p, cols.data(), sizeof(TcCol) * ncols,
+                               cudaMemcpyHostToDevice, stream));
+  DBX_CUDA_TRY(cudaMemcpyAsync(st->mcb.p, model_col_begin.data(),
+                               sizeof(int) * (nmodels + 1), cudaMemcpyHostToDevice,
+                               stream));
+  st->h2d += sizeof(TcTile) * ntiles + sizeof(TcCol) * ncols + sizeof(int) * (nmodels + 1);
+  DBX_CUDA_TRY(cudaMemsetAsync(st->nonself.p, 0, sizeof(int) * ncols, stream));
+  DBX_CUDA_TRY(cudaMemsetAsync(st->err.p, 0, sizeof(int), stream));
+  self_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>((TcCol *)st->cols.p, ncols,
+                                                       rstep);
+  const long long nwarps = (long long)ntiles * kTN;
+  weights_kernel<<<(unsigned)((nwarps * 32 + 255) / 256), 256, 0, stream>>>(
+      (const TcTile *)st->tiles.p, ntiles, (const TcCol *)st->cols.p, rstep,
+      (__nv_bfloat16 *)st->W.p, (int *)st->E.p, (int *)st->nonself.p);
+  DBX_CUDA_TRY(cudaGetLastError());
+  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kSmemBytes));
+  tm->start(DBX_T_DEBYE, stream);
+  gemm_kernel<<<nrt * ntiles, kThreads, kSmemBytes, stream>>>(
+      (const __nv_bfloat16 *)st->basis.p, (const __nv_bfloat16 *)st->W.p,
+      (const TcTile *)st->tiles.p, (const int *)st->E.p, (const float4 *)st->twid.p,
+      Qp, nrt, (double *)st->P.p, (int *)st->err.p);
+  DBX_CUDA_TRY(cudaGetLastError());
+  tm->stop(DBX_T_DEBYE, stream);
+  dim3 rg((nq + 127) / 128, nmodels);
+  reduce_kernel<<<rg, 128, 0, stream>>>(
+      (const TcCol *)st->cols.p, ncols, (const int *)st->mcb.p, nmodels,
+      (const double *)st->P.p, (const int *)st->nonself.p, d_K, nq, Qp, d_I);
+  DBX_CUDA_TRY(cudaGetLastError());
+  int herr = 0;
+  DBX_CUDA_TRY(cudaMemcpyAsync(&herr, st->err.p, sizeof(int), cudaMemcpyDeviceToHost,
+                               stream));
+  DBX_CUDA_TRY(cudaStreamSynchronize(stream));
+  st->d2h += sizeof(int);
+  if (herr)
+    return fail(DBX_ERR_TIMEOUT, "tensor-core contraction: a bounded device wait ran out");
+  return ok();
+}
+
+}  // namespace dbx

@@ -1,0 +1,38 @@
+// debye_tc.h — tensor-core Debye contraction (debye_tc.cu).
+#pragma once
+#include <vector>
+
+#include "engine.h"
+
+namespace dbx {
+
+struct TcTile {  // 64 consecutive chunks of one column
+  int col, ch0, pad0, pad1;
+};
+
+struct TcCol {  // one (model, species pair) column of the contraction
+  const unsigned long long *hist;  // device counts [nbins]
+  long long nbins;
+  const double *ff;                // device prefactor [nq]
+  int tile_begin, tile_end;        // filled by debye_tc
+  double self;                     // self-distance sum, filled on the device
+};
+
+struct TcState {  // cached plan data (basis, twiddles) and workspace
+  DevBuf basis, twid, W, E, P, tiles, cols, mcb, nonself, err;
+  std::vector<double> grid_K;
+  double grid_rstep = 0;
+  int grid_nch = 0;
+  int64_t h2d = 0, d2h = 0;
+};
+
+// I[model][q] for the columns grouped by model (model_col_begin has
+// nmodels+1 offsets into cols, columns of a model in pair order).
+Error debye_tc(TcState *st, std::vector<TcCol> cols,
+               const std::vector<int> &model_col_begin, double rstep,
+               const double *h_K, const double *d_K, int nq, double *d_I,
+               cudaStream_t stream, size_t *bytes_delta, Timers *tm);
+void tc_release(TcState *st);
+size_t tc_bytes(const TcState *st);
+
+}  // namespace dbx

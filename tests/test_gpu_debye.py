@@ -59,6 +59,52 @@ def test_tc_precision(engine, orc):
     assert rel.max() <= 1e-6, rel.max()
 
 
+def test_tc_multi_tile_and_ragged_q(engine, orc):
+    """nq not a multiple of 128, columns spanning several 64-chunk tiles
+    (>16,384 bins), and a second call on the cached basis."""
+    m = lattice.spinel(radius=20.0, target=6000, seed=23)
+    tt, K = m.k_grid()
+    for Kq in (K[::3], K[5::3]):
+        got, want = _model_case(engine, orc, m, Kq, "tc")
+        rel = np.abs(got - want) / np.abs(want)
+        assert rel.max() <= 1e-6, rel.max()
+
+
+def test_tc_precision_grid(engine, orc):
+    """The 20,000-point q grid (2theta 5-150 deg at 0.7107 A, K up to 17)."""
+    m = lattice.spinel(radius=20.0, target=6000, seed=24,
+                       grid=lattice.GRID_PRECISION)
+    tt, K = m.k_grid()
+    assert len(K) == 20000
+    got, want = _model_case(engine, orc, m, K[::4], "tc")
+    rel = np.abs(got - want) / np.abs(want)
+    assert rel.max() <= 1e-6, rel.max()
+
+
+def test_tc_self_only_and_zero_q(engine, orc):
+    """Single-atom species have only the self bin; K = 0 gives the
+    reference's NaN only where a non-self bin exists."""
+    xyz = np.array([[0, 0, 0], [1.5, 0, 0]], np.float32)
+    sp = [lattice.species("O", 1.0, 0.5), lattice.species("Al", 1.0, 0.5)]
+    K = np.array([0.0, 0.5, 3.0])
+    mod = engine.upload(xyz, [1, 1])
+    try:
+        got = engine.intensity(mod, 1e-3, cd.channels(4, 1e-3), sp, K, mode="tc")
+        h = engine.histogram(mod, 1e-3, cd.channels(4, 1e-3))
+    finally:
+        mod.free()
+    want = orc.intensity(K, h, sp, 1e-3)
+    assert np.isnan(want[0]) and np.isnan(got[0])
+    np.testing.assert_allclose(got[1:], want[1:], rtol=1e-6)
+    mod = engine.upload(xyz[:1], [1])
+    try:
+        got = engine.intensity(mod, 1e-3, 10, sp[:1], K, mode="tc")
+    finally:
+        mod.free()
+    want = orc.prefactor(K, sp[0], sp[0]) * 1.0
+    np.testing.assert_allclose(got, want, rtol=1e-12)
+
+
 def test_fp32_plain_form_runs(engine, orc):
     m = lattice.plain_small()
     tt, K = m.k_grid()
