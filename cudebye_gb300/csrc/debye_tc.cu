@@ -235,6 +235,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "r"(taddr));
 }
 
+// Completes all prior tcgen05.ld of this thread. The loaded registers are
+// passed through as in/out operands so that the compiler cannot use them
+// before the wait.
+__device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]),
+                 "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]),
+                 "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
+                 "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+
 __global__ void __launch_bounds__(kThreads, 2)
     gemm_kernel(const __nv_bfloat16 *__restrict__ A,
                 const __nv_bfloat16 *__restrict__ W,
@@ -344,14 +357,22 @@ __global__ void __launch_bounds__(kThreads, 2)
       tmem_ld16(lane_base + 1 * kTN + cg * 16, a1);
       tmem_ld16(lane_base + 2 * kTN + cg * 16, a2);
       tmem_ld16(lane_base + 3 * kTN + cg * 16, a3);
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      tmem_wait16(a0);
+      tmem_wait16(a1);
+      tmem_wait16(a2);
+      tmem_wait16(a3);
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int n = cg * 16 + i;
-        const float hi = __uint_as_float(a0[i]);
-        const float lo = fmaf(__uint_as_float(a1[i]), 0x1p-8f,
-                              fmaf(__uint_as_float(a2[i]), 0x1p-16f,
-                                   __uint_as_float(a3[i]) * 0x1p-24f));
+        // D = acc0 + acc1 2^-8 + acc2 2^-16 + acc3 2^-24 (exact integers):
+        // exact two-sum of the top two classes, the rest rounded once.
+        const float c0 = __uint_as_float(a0[i]);
+        const float c1 = __uint_as_float(a1[i]) * 0x1p-8f;
+        const float hi = c0 + c1;
+        const float hb = hi - c0;
+        const float lo = ((c0 - (hi - hb)) + (c1 - hb)) +
+                         fmaf(__uint_as_float(a2[i]), 0x1p-16f,
+                              __uint_as_float(a3[i]) * 0x1p-24f);
         const float4 t = twq[(size_t)(tile.ch0 + n) * Qp];
         const float th = sinrow ? t.z : t.x;
         const float tl = sinrow ? t.w : t.y;
