@@ -159,7 +159,7 @@ __global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   int e = 0;
   if (mx > 0.0) frexp(mx, &e);  // mx < 2^e
-  const double scale = ldexp(1.0, 31 - e);
+  const double scale = ldexp(1.0, -e);  // |w * scale| < 1; fixed31 adds 2^31
   const int j0 = lane * 8, ks = j0 / kKS, k0 = j0 % kKS;
   const size_t base = (size_t)(nt * kNSlab + ks) * kND * kBBlock + tiled_off(n, k0);
   alignas(16) __nv_bfloat16 dig[kND][8];
