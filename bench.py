@@ -113,9 +113,20 @@ def dist_env():
     return ws, rank, local
 
 
+WORKLOADS = {
+    # the metric's configuration: ~118k-atom spinel-like 10 nm particle
+    "spinel_10nm": lambda L: L.spinel_10nm(),
+    # smaller cases of the same kernels, for profiler captures
+    "spinel_medium": lambda L: L.spinel(radius=30.0, target=25000, seed=7,
+                                        label="spinel_medium"),
+    "plain_small": lambda L: L.plain_small(),
+}
+WORKLOAD = "spinel_10nm"
+
+
 def workload():
     from cudebye_gb300 import lattice
-    return lattice.spinel_10nm()
+    return WORKLOADS[WORKLOAD](lattice)
 
 
 def cpu_baseline(m, K, budget_s=12.0, threads=0):
@@ -182,7 +193,7 @@ def run_reference(args):
         "ms_per_step": b["pattern_s"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded spinel-like nanoparticle)",
-        "config": {"workload": "spinel_10nm", "atoms": m.natoms,
+        "config": {"workload": m.label, "atoms": m.natoms,
                    "species": len(m.counts), "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
                    "bins": m.nbins, "rstep": m.rstep, "q_points": len(K),
                    "binned_pairs": m.pairs, "parallelism": "replicas",
@@ -306,7 +317,7 @@ def run_engine(args):
         "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded spinel-like nanoparticle)",
-        "config": {"workload": "spinel_10nm", "atoms": m.natoms,
+        "config": {"workload": m.label, "atoms": m.natoms,
                    "species": len(m.counts), "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
                    "bins": m.nbins, "rstep": m.rstep, "q_points": len(K),
                    "binned_pairs": m.pairs, "debye_mode": mode,
@@ -341,7 +352,11 @@ def main():
     ap.add_argument("--mode", default="tc", choices=["tc", "fp64", "fp32"])
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--workload", default="spinel_10nm",
+                    choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = args.workload
     if args.impl == "reference":
         return run_reference(args)
     return run_engine(args)
