@@ -10,7 +10,7 @@
 //  * A CTA owns a window of up to ~114k bins held in shared memory as packed
 //    16-bit counters (two bins per 32-bit word). A counter that wraps is
 //    detected from the atomic's return value and compensated exactly in the
-//    int64 global histogram (see add16), so the counts stay exact.
+//    int64 global histogram (see wrap16), so the counts stay exact.
 //  * Tile pairs are grouped into (species pair, bin window) segments from
 //    their bounding boxes, and split into equal CTA tasks. Each task writes
 //    its packed window once to a scratch slot; a reduce kernel sums the slots
@@ -18,7 +18,7 @@
 //  * The distance and bin are the reference's FP32 formula, unfused
 //    (cuDebye-v15.cu:101-107): IEEE sqrt, explicit _rn intrinsics so that
 //    nothing is contracted to FMA, and roundf computed exactly without a
-//    float->int conversion (exact_bin).
+//    float->int conversion (bin1).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,47 +28,75 @@
 
 namespace dbx {
 
-constexpr int kHistThreads = 1024;
+constexpr int kHistThreads = 512;
 // Dynamic shared memory per CTA for the window (bytes); 1 CTA per SM.
 constexpr int kHistSmemBytes = 224 * 1024;
 constexpr int kWindowBins = (kHistSmemBytes / 4) * 2;  // 114688, even
 
 int hist_window_bins() { return kWindowBins; }
 
-// Exact bin of one pair: (int)roundf(sqrtf((dx*dx + dy*dy) + dz*dz) * inv)
-// with every operation rounded separately (cuDebye-v15.cu:101-107, :115).
-// roundf(p) for 0 <= p < 2^23: t = p + 2^23 rounds p to an integer with
-// ties-to-even; the bits of t minus those of 2^23 are that integer; a tie
-// (p - round_even(p) == 0.5) is moved up, giving round-half-away-from-zero.
-// p >= 2^23, inf or NaN give an index >= 2^23 (or negative), which the
-// caller treats as out of range.
-__device__ __forceinline__ int exact_bin(float ax, float ay, float az,
-                                         float4 b, float inv) {
-  const float dx = __fsub_rn(b.x, ax);
-  const float dy = __fsub_rn(b.y, ay);
-  const float dz = __fsub_rn(b.z, az);
+// ---- packed FP32x2 subtraction (sm_100+): two independent IEEE
+// round-to-nearest subtractions per instruction. Only the coordinate
+// differences use it: a packed multiply followed by a packed add was
+// observed to be contracted into a fused operation by the compiler back end
+// despite the explicit rounding modifier, which changes the reference's
+// unfused result; the scalar _rn intrinsics below are never contracted.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float lo, float hi) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk(f2 v, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+  f2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
+// Exact bin of one pair from its coordinate differences:
+// (int)roundf(sqrtf((dx*dx + dy*dy) + dz*dz) * inv), every operation
+// rounded separately (cuDebye-v15.cu:101-107, :115). roundf(p) for
+// 0 <= p < 2^23 needs no float->int conversion: t = p + 2^23 rounds p to an
+// integer with ties-to-even, the bits of t minus those of 2^23 are that
+// integer, and a tie (p - round_even(p) == 0.5) is moved up, giving
+// round-half-away-from-zero. p >= 2^23, inf or NaN give an index >= 2^23
+// (or negative), which the caller treats as out of range.
+__device__ __forceinline__ int bin1(float dx, float dy, float dz, float inv) {
   float s = __fmul_rn(dx, dx);
   s = __fadd_rn(s, __fmul_rn(dy, dy));
   s = __fadd_rn(s, __fmul_rn(dz, dz));
   const float p = __fmul_rn(__fsqrt_rn(s), inv);
   const float t = __fadd_rn(p, 8388608.0f);
-  int k = __float_as_int(t) - 0x4B000000;
   const float r = __fsub_rn(t, 8388608.0f);
-  k += (__fsub_rn(p, r) == 0.5f) ? 1 : 0;
-  return k;
+  return __float_as_int(t) - 0x4B000000 + (__fsub_rn(p, r) == 0.5f ? 1 : 0);
 }
 
-// Add one count to bin lk of the packed 16-bit shared window. When the add
-// wraps a 16-bit half (seen in the returned old value), credit 65536 to that
-// bin in the global int64 histogram; a wrap of the low half also carried 1
-// into the high half (bin lk+1), which is debited there, and if that carry
-// wrapped the high half as well it is credited too. Every wrap is seen by
-// exactly one thread (the one whose atomic caused it), so
-// count = stored + 65536*wraps - carries holds exactly.
-__device__ __forceinline__ void add16(unsigned *sh, unsigned lk,
-                                      unsigned long long *gh) {
+// Bins of two row atoms (packed coordinates) against one column atom.
+__device__ __forceinline__ void bins2(f2 X, f2 Y, f2 Z, f2 bx, f2 by, f2 bz,
+                                      float inv, int &k0, int &k1) {
+  float dx0, dx1, dy0, dy1, dz0, dz1;
+  upk(sub2(bx, X), dx0, dx1);
+  upk(sub2(by, Y), dy0, dy1);
+  upk(sub2(bz, Z), dz0, dz1);
+  k0 = bin1(dx0, dy0, dz0, inv);
+  k1 = bin1(dx1, dy1, dz1, inv);
+}
+
+// The window holds packed 16-bit counters, two bins per 32-bit word. A
+// count is added with one atomicAdd of 1 (even bin, low half) or 0x10000
+// (odd bin, high half); its returned old value shows whether that add
+// wrapped a 16-bit half. Then credit 65536 to that bin in the global int64
+// histogram; a wrap of the low half also carried 1 into the high half (bin
+// lk+1), which is debited there, and if that carry wrapped the high half as
+// well it is credited too. Every wrap is seen by exactly one thread (the one
+// whose atomic caused it), so count = stored + 65536*wraps - carries holds
+// exactly.
+__device__ __forceinline__ void wrap16(unsigned old, unsigned lk,
+                                       unsigned long long *gh) {
   const unsigned sh16 = (lk & 1u) << 4;
-  const unsigned old = atomicAdd(&sh[lk >> 1], 1u << sh16);
   if (((old >> sh16) & 0xFFFFu) == 0xFFFFu) {
     atomicAdd(&gh[lk], 65536ull);
     if (sh16 == 0) {
@@ -78,6 +106,10 @@ __device__ __forceinline__ void add16(unsigned *sh, unsigned lk,
   }
 }
 
+// One warp = one tile pair (128 x 128 atoms): each lane holds four row
+// atoms (lane + 32r) and streams the column tile; each column atom is one
+// warp-uniform 16-byte load serving four pairs. CTAs pull equal-sized tasks
+// from a global counter; task t's packed window goes to partial slot t.
 __global__ void __launch_bounds__(kHistThreads, 1)
     hist_tiles_kernel(const float4 *__restrict__ atoms,
                       const int2 *__restrict__ tiles,
@@ -87,12 +119,17 @@ __global__ void __launch_bounds__(kHistThreads, 1)
                       unsigned nbins, unsigned *__restrict__ partial,
                       int words_per_task, unsigned long long *__restrict__ hist,
                       long long pitch,
-                      unsigned long long *__restrict__ oor_total) {
+                      unsigned long long *__restrict__ oor_total,
+                      int *__restrict__ task_counter) {
   extern __shared__ unsigned sh[];
   __shared__ unsigned s_oor;
+  __shared__ int s_task;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int kSub = kTile / 32;  // warp sub-blocks per tile
-  for (int t = blockIdx.x; t < ntasks; t += gridDim.x) {
+  for (;;) {
+    if (threadIdx.x == 0) s_task = atomicAdd(task_counter, 1);
+    __syncthreads();
+    const int t = s_task;
+    if (t >= ntasks) break;
     const HistTask tk = tasks[t];
     const HistSeg sg = segs[tk.seg];
     const int nw = (sg.wl + 1) >> 1;
@@ -100,34 +137,54 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     if (threadIdx.x == 0) s_oor = 0u;
     __syncthreads();
     unsigned long long *gh = hist + (long long)sg.pair * pitch + sg.kb;
+    const unsigned wl = (unsigned)sg.wl, kb = (unsigned)sg.kb;
     unsigned my_oor = 0;
-    const int nunits = (tk.item_end - tk.item_begin) * kSub;
-    for (int u = warp; u < nunits; u += kHistThreads / 32) {
-      const int2 it = __ldg(&items[tk.item_begin + u / kSub]);
-      const int sub = u % kSub;
+    for (int it_i = tk.item_begin + warp; it_i < tk.item_end;
+         it_i += kHistThreads / 32) {
+      const int2 it = __ldg(&items[it_i]);
       const bool diag = it.y < 0;
       const int2 TI = __ldg(&tiles[it.x]);
       const int2 TJ = __ldg(&tiles[it.y & 0x7fffffff]);
-      if (sub * 32 >= TI.y) continue;  // warp-uniform: empty sub-block
-      const int pi = sub * 32 + lane;
-      const bool active = pi < TI.y;
-      const float4 a = __ldg(&atoms[TI.x + (active ? pi : TI.y - 1)]);
-      // diag tile (same tile, same species): pairs j <= i incl. i == j,
-      // the reference's `dist` kernel (cuDebye-v15.cu:137).
-      const int jend_lane = active ? (diag ? pi + 1 : TJ.y) : 0;
-      const int jend = diag ? min(TJ.y, sub * 32 + 32) : TJ.y;
+      // row atoms lane + 32r; jlim: last column index paired with it
+      float x[4], y[4], z[4];
+      int jlim[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int pi = lane + 32 * r;
+        const bool act = pi < TI.y;
+        const float4 a = __ldg(&atoms[TI.x + (act ? pi : 0)]);
+        x[r] = a.x;
+        y[r] = a.y;
+        z[r] = a.z;
+        // diag tile: pairs j <= i incl. i == j (cuDebye-v15.cu:137)
+        jlim[r] = act ? (diag ? pi : 0x7fffffff) : -1;
+      }
+      const f2 X01 = pk(x[0], x[1]), X23 = pk(x[2], x[3]);
+      const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
+      const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
       const float4 *bj = atoms + TJ.x;
-#pragma unroll 4
+      const int jend = TJ.y;
+#pragma unroll 2
       for (int j = 0; j < jend; ++j) {
-        const float4 b = __ldg(&bj[j]);  // warp-uniform address: broadcast
-        if (j < jend_lane) {
-          const int k = exact_bin(a.x, a.y, a.z, b, inv);
-          const unsigned lk = (unsigned)(k - sg.kb);
-          if (lk < (unsigned)sg.wl)
-            add16(sh, lk, gh);
-          else if ((unsigned)k >= nbins)
-            ++my_oor;
+        const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
+        const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
+        int k[4];
+        bins2(X01, Y01, Z01, bx, by, bz, inv, k[0], k[1]);
+        bins2(X23, Y23, Z23, bx, by, bz, inv, k[2], k[3]);
+        unsigned old[4], lk[4];
+        bool hit[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const bool valid = j <= jlim[r];
+          lk[r] = (unsigned)k[r] - kb;
+          hit[r] = valid && lk[r] < wl;
+          my_oor += (valid && !hit[r] && (unsigned)k[r] >= nbins) ? 1u : 0u;
+          old[r] = hit[r] ? atomicAdd(&sh[lk[r] >> 1], (lk[r] & 1u) ? 0x10000u : 1u)
+                          : 0u;
         }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+          if (hit[r]) wrap16(old[r], lk[r], gh);
       }
     }
     my_oor = __reduce_add_sync(0xffffffffu, my_oor);
@@ -249,21 +306,26 @@ Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
     const int64_t na = m.sp_count[a], nb = m.sp_count[b];
     plan->pairs += (a == b) ? na * (na + 1) / 2 : na * nb;
   }
-  // Split segments into about target_tasks tasks of equal pair counts.
+  // Split every segment into n_s tasks of about equal pair counts, n_s
+  // from the segment's share of about target_tasks tasks in all.
   int64_t total = 0;
   for (int64_t v : seg_pairs) total += v;
-  const int64_t target =
-      std::max<int64_t>(total / std::max(1, target_tasks), 1);
+  const double target =
+      std::max(1.0, (double)total / std::max(1, target_tasks));
   for (size_t s = 0; s < plan->segs.size(); ++s) {
     HistSeg &sg = plan->segs[s];
     sg.task_begin = (int)plan->tasks.size();
-    int64_t acc = 0;
-    int begin = seg_items[s].x;
-    for (int i = seg_items[s].x; i < seg_items[s].y; ++i) {
+    const int i0 = seg_items[s].x, i1 = seg_items[s].y;
+    const int64_t n_s = std::max<int64_t>(
+        1, std::min<int64_t>(i1 - i0, (int64_t)std::llround(seg_pairs[s] / target)));
+    int64_t acc = 0, k = 1;
+    int begin = i0;
+    for (int i = i0; i < i1; ++i) {
       const int2 it = plan->items[i];
       const int2 TI = m.tiles[it.x], TJ = m.tiles[it.y & 0x7fffffff];
       acc += item_pairs(TI.y, TJ.y, it.y < 0);
-      if (acc >= target || i + 1 == seg_items[s].y) {
+      // close task k when the running sum reaches k/n_s of the segment
+      if (i + 1 == i1 || (k < n_s && acc * n_s >= k * seg_pairs[s])) {
         HistTask t;
         t.seg = (int)s;
         t.item_begin = begin;
@@ -271,7 +333,7 @@ Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
         t.pad = 0;
         plan->tasks.push_back(t);
         begin = i + 1;
-        acc = 0;
+        ++k;
       }
     }
     sg.task_end = (int)plan->tasks.size();
@@ -308,7 +370,7 @@ Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
   DBX_TRY(ensure(&ws->tasks, std::max(ntasks, 1) * sizeof(HistTask), ws_bytes_delta));
   DBX_TRY(ensure(&ws->partial, std::max<size_t>((size_t)ntasks * words, 1) * 4,
                  ws_bytes_delta));
-  DBX_TRY(ensure(&ws->oor, sizeof(unsigned long long), ws_bytes_delta));
+  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
   DBX_CUDA_TRY(cudaMemsetAsync(
       d_out, 0, sizeof(unsigned long long) * (size_t)pitch * plan.nrows, stream));
   if (ntasks == 0) return ok();
@@ -321,7 +383,8 @@ Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
   DBX_CUDA_TRY(cudaMemcpyAsync(ws->tasks.p, plan.tasks.data(),
                                ntasks * sizeof(HistTask),
                                cudaMemcpyHostToDevice, stream));
-  DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, sizeof(unsigned long long), stream));
+  // oor counter and the task counter share one 16-byte buffer
+  DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, 2 * sizeof(unsigned long long), stream));
   const int smem = words * 4;
   DBX_CUDA_TRY(cudaFuncSetAttribute(hist_tiles_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -332,7 +395,8 @@ Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
       m.d_atoms, m.d_tiles, (const int2 *)ws->items.p,
       (const HistTask *)ws->tasks.p, ntasks, (const HistSeg *)ws->segs.p,
       inv_rstep, (unsigned)nbins, (unsigned *)ws->partial.p, words, d_out,
-      (long long)pitch, (unsigned long long *)ws->oor.p);
+      (long long)pitch, (unsigned long long *)ws->oor.p,
+      (int *)((unsigned long long *)ws->oor.p + 1));
   DBX_CUDA_TRY(cudaGetLastError());
   tm->stop(DBX_T_HIST, stream);
   tm->start(DBX_T_HIST_REDUCE, stream);
