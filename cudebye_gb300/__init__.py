@@ -36,7 +36,7 @@ ERRORS = {
     -1: "DBX_ERR_ARG", -2: "DBX_ERR_CUDA", -3: "DBX_ERR_NOMEM",
     -4: "DBX_ERR_FILE", -5: "DBX_ERR_PARSE", -6: "DBX_ERR_COUNT",
     -7: "DBX_ERR_RANGE", -8: "DBX_ERR_MODEL", -9: "DBX_ERR_TIMEOUT",
-    -10: "DBX_ERR_IO",
+    -10: "DBX_ERR_IO", -11: "DBX_ERR_LIMIT",
 }
 MODES = {"tc": 0, "fp64": 1, "fp32": 2}
 
@@ -47,7 +47,7 @@ EXPORTS = (
     "dbx_pair_histogram", "dbx_histogram", "dbx_channels", "dbx_reduce_check",
     "dbx_k_grid", "dbx_atomic_prop", "dbx_intensity", "dbx_pattern",
     "dbx_set_stream", "dbx_set_timing", "dbx_get_timing", "dbx_get_traffic",
-    "dbx_run_deb",
+    "dbx_run_deb", "dbx_pair_histogram_noalloc",
 )
 TIMERS = ("hist", "hist_reduce", "prefactor", "debye")
 
@@ -131,6 +131,9 @@ def load_library(path=None):
         "dbx_get_traffic": (ctypes.c_int, [c_p, i64p]),
         "dbx_run_deb": (ctypes.c_int, [c_p, ctypes.c_char_p, ctypes.c_char_p,
                                        ctypes.c_int]),
+        "dbx_pair_histogram_noalloc": (ctypes.c_int, [
+            c_p, c_p, c_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+            ctypes.c_int64, ctypes.c_double, ctypes.c_int64, c_p, c_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

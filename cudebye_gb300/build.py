@@ -25,8 +25,9 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
           "-Xcompiler", "-Wall", "-I", INCLUDE]
 # Per-file flags. hist.cu must never contract the reference's unfused FP32
 # distance arithmetic into FMAs (it also uses explicit _rn intrinsics).
-EXTRA = {"hist.cu": ["--fmad=false"]}
-LIB_SOURCES = ["hist.cu", "debye.cu", "debye_tc.cu", "capi.cu", "debio.cpp"]
+EXTRA = {"hist.cu": ["--fmad=false"], "hist_noalloc.cu": ["--fmad=false"]}
+LIB_SOURCES = ["hist.cu", "hist_noalloc.cu", "debye.cu", "debye_tc.cu",
+               "capi.cu", "debio.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 
 

@@ -206,6 +206,8 @@ const char *dbx_strerror(int code) {
     case DBX_ERR_MODEL: return "unknown model id";
     case DBX_ERR_TIMEOUT: return "device wait timed out";
     case DBX_ERR_IO: return "output file could not be written";
+    case DBX_ERR_LIMIT:
+      return "request exceeds the fixed scratch of the no-allocation entry point";
     default: return "unknown error";
   }
 }

@@ -25,6 +25,7 @@
 #include <cmath>
 
 #include "engine.h"
+#include "hist_device.cuh"
 
 namespace dbx {
 
@@ -34,77 +35,6 @@ constexpr int kHistSmemBytes = 224 * 1024;
 constexpr int kWindowBins = (kHistSmemBytes / 4) * 2;  // 114688, even
 
 int hist_window_bins() { return kWindowBins; }
-
-// ---- packed FP32x2 subtraction (sm_100+): two independent IEEE
-// round-to-nearest subtractions per instruction. Only the coordinate
-// differences use it: a packed multiply followed by a packed add was
-// observed to be contracted into a fused operation by the compiler back end
-// despite the explicit rounding modifier, which changes the reference's
-// unfused result; the scalar _rn intrinsics below are never contracted.
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 pk(float lo, float hi) {
-  f2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void upk(f2 v, float &lo, float &hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-  f2 r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-
-// Exact bin of one pair from its coordinate differences:
-// (int)roundf(sqrtf((dx*dx + dy*dy) + dz*dz) * inv), every operation
-// rounded separately (cuDebye-v15.cu:101-107, :115). roundf(p) for
-// 0 <= p < 2^23 needs no float->int conversion: t = p + 2^23 rounds p to an
-// integer with ties-to-even, the bits of t minus those of 2^23 are that
-// integer, and a tie (p - round_even(p) == 0.5) is moved up, giving
-// round-half-away-from-zero. p >= 2^23, inf or NaN give an index >= 2^23
-// (or negative), which the caller treats as out of range.
-__device__ __forceinline__ int bin1(float dx, float dy, float dz, float inv) {
-  float s = __fmul_rn(dx, dx);
-  s = __fadd_rn(s, __fmul_rn(dy, dy));
-  s = __fadd_rn(s, __fmul_rn(dz, dz));
-  const float p = __fmul_rn(__fsqrt_rn(s), inv);
-  const float t = __fadd_rn(p, 8388608.0f);
-  const float r = __fsub_rn(t, 8388608.0f);
-  return __float_as_int(t) - 0x4B000000 + (__fsub_rn(p, r) == 0.5f ? 1 : 0);
-}
-
-// Bins of two row atoms (packed coordinates) against one column atom.
-__device__ __forceinline__ void bins2(f2 X, f2 Y, f2 Z, f2 bx, f2 by, f2 bz,
-                                      float inv, int &k0, int &k1) {
-  float dx0, dx1, dy0, dy1, dz0, dz1;
-  upk(sub2(bx, X), dx0, dx1);
-  upk(sub2(by, Y), dy0, dy1);
-  upk(sub2(bz, Z), dz0, dz1);
-  k0 = bin1(dx0, dy0, dz0, inv);
-  k1 = bin1(dx1, dy1, dz1, inv);
-}
-
-// The window holds packed 16-bit counters, two bins per 32-bit word. A
-// count is added with one atomicAdd of 1 (even bin, low half) or 0x10000
-// (odd bin, high half); its returned old value shows whether that add
-// wrapped a 16-bit half. Then credit 65536 to that bin in the global int64
-// histogram; a wrap of the low half also carried 1 into the high half (bin
-// lk+1), which is debited there, and if that carry wrapped the high half as
-// well it is credited too. Every wrap is seen by exactly one thread (the one
-// whose atomic caused it), so count = stored + 65536*wraps - carries holds
-// exactly.
-__device__ __forceinline__ void wrap16(unsigned old, unsigned lk,
-                                       unsigned long long *gh) {
-  const unsigned sh16 = (lk & 1u) << 4;
-  if (((old >> sh16) & 0xFFFFu) == 0xFFFFu) {
-    atomicAdd(&gh[lk], 65536ull);
-    if (sh16 == 0) {
-      atomicAdd(&gh[lk + 1], ~0ull);  // -1 for the carry
-      if ((old >> 16) == 0xFFFFu) atomicAdd(&gh[lk + 1], 65536ull);
-    }
-  }
-}
 
 // One warp = one tile pair (128 x 128 atoms): each lane holds four row
 // atoms (lane + 32r) and streams the column tile; each column atom is one

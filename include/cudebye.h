@@ -43,6 +43,8 @@ extern "C" {
 #define DBX_ERR_MODEL (-8)    /* unknown model id */
 #define DBX_ERR_TIMEOUT (-9)  /* a bounded device-side wait ran out */
 #define DBX_ERR_IO (-10)      /* output file could not be written */
+#define DBX_ERR_LIMIT (-11)   /* request exceeds the fixed scratch of
+                                 dbx_pair_histogram_noalloc */
 
 typedef struct dbx_ctx dbx_ctx;
 
@@ -101,6 +103,40 @@ int dbx_pair_histogram(dbx_ctx *ctx, int64_t model_id, int row, int col,
  * [npairs][nbins] in pair order (the pair loop cuDebye-v15.cu:941-967). */
 int dbx_histogram(dbx_ctx *ctx, int64_t model_id, double rstep, int64_t nbins,
                   int64_t *out_counts);
+
+/* Pair histogram for callers that cannot allocate device memory. No
+ * counterpart in the reference (its splitCalcDist allocates with cudaMalloc
+ * on every call, cuDebye-v15.cu:196-198).
+ *
+ * Who needs it: code running inside another framework's memory pool or a
+ * fixed arena it must not grow, plugins in a host process that owns every
+ * device allocation, and services that forbid device allocation once they
+ * are up. This call allocates nothing: no cudaMalloc, no cudaFree, no
+ * allocating library routine. All its scratch lives in one fixed 64 MiB
+ * __device__ array that every GPU loading this library holds until the
+ * process exits.
+ *
+ * Inputs are the reference's device arrays and index ranges: x, y, z
+ * (float, device) and the atom ranges [a_start, a_start+a_count) and
+ * [b_start, b_start+b_count); a range paired with itself (a_start ==
+ * b_start and equal counts) counts pairs j <= i including i == j, like the
+ * reference's `dist` kernel. out (int64, device, nbins entries) receives
+ * the histogram, bit-exact with dbx_pair_histogram. stream is a
+ * cudaStream_t (NULL: the legacy default stream); the call returns after
+ * the stream has finished it.
+ *
+ * Limits: at most DBX_NOALLOC_MAX_ATOMS atoms (a_count + b_count, or a_count
+ * for a range with itself), else DBX_ERR_LIMIT; nbins <= 4194304.
+ * The first call on a device looks up the scratch array's device address
+ * (with that device current), so make it before any stream capture. All
+ * calls share the array and leave their data in it; each call clears what
+ * must start at zero. Calls that overlap on the GPU race on the array: order
+ * them (one stream, or events). */
+#define DBX_NOALLOC_MAX_ATOMS 1834992
+int dbx_pair_histogram_noalloc(const float *x, const float *y, const float *z,
+                               int64_t a_start, int64_t a_count,
+                               int64_t b_start, int64_t b_count, double rstep,
+                               int64_t nbins, int64_t *out, void *stream);
 
 /* int(rmax/rstep)+2 (cuDebye-v15.cu:732). */
 int64_t dbx_channels(double rmax, double rstep);
