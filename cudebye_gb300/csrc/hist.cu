@@ -18,7 +18,7 @@
 //  * The distance and bin are the reference's FP32 formula, unfused
 //    (cuDebye-v15.cu:101-107): IEEE sqrt, explicit _rn intrinsics so that
 //    nothing is contracted to FMA, and roundf computed exactly without a
-//    float->int conversion (bin1).
+//    float->int conversion (bin_rel).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,16 +29,62 @@
 
 namespace dbx {
 
-constexpr int kHistThreads = 512;
+constexpr int kHistThreads = 1024;
 // Dynamic shared memory per CTA for the window (bytes); 1 CTA per SM.
 constexpr int kHistSmemBytes = 224 * 1024;
 constexpr int kWindowBins = (kHistSmemBytes / 4) * 2;  // 114688, even
 
 int hist_window_bins() { return kWindowBins; }
 
-// One warp = one tile pair (128 x 128 atoms): each lane holds four row
-// atoms (lane + 32r) and streams the column tile; each column atom is one
-// warp-uniform 16-byte load serving four pairs. CTAs pull equal-sized tasks
+// The column-atom loop of one tile pair for one warp: lanes hold four row
+// atoms; each column atom is one warp-uniform 16-byte load serving four
+// pairs. kAllValid: a full 128 x 128 off-diagonal tile pair (no per-pair
+// validity test). kFullWindow: the window covers bins [0, nbins), so a
+// valid pair that misses it is out of range.
+template <bool kAllValid, bool kFullWindow>
+__device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
+                                          int jend, const float (&x)[4],
+                                          const float (&y)[4],
+                                          const float (&z)[4],
+                                          const int (&jlim)[4], float inv,
+                                          unsigned base, unsigned wl,
+                                          unsigned kb, unsigned nbins,
+                                          unsigned *sh, unsigned long long *gh,
+                                          unsigned &my_oor) {
+  const f2 X01 = pk(x[0], x[1]), X23 = pk(x[2], x[3]);
+  const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
+  const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
+#pragma unroll 2
+  for (int j = 0; j < jend; ++j) {
+    const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
+    const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
+    unsigned lk[4], old[4];
+    bins2(X01, Y01, Z01, bx, by, bz, inv, base, lk[0], lk[1]);
+    bins2(X23, Y23, Z23, bx, by, bz, inv, base, lk[2], lk[3]);
+    bool hit[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const bool valid = kAllValid || j <= jlim[r];
+      hit[r] = valid && lk[r] < wl;
+      if (kFullWindow)
+        my_oor += (valid && !hit[r]) ? 1u : 0u;
+      else
+        my_oor += (valid && !hit[r] && lk[r] + kb >= nbins) ? 1u : 0u;
+      old[r] = hit[r] ? atomicAdd(&sh[lk[r] >> 1], (lk[r] & 1u) ? 0x10000u : 1u)
+                      : 0u;
+    }
+    bool w[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) w[r] = hit[r] && wrapped16(old[r], lk[r]);
+    if (w[0] | w[1] | w[2] | w[3]) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        if (w[r]) wrap16(old[r], lk[r], gh);
+    }
+  }
+}
+
+// One warp = one tile pair (128 x 128 atoms). CTAs pull equal-sized tasks
 // from a global counter; task t's packed window goes to partial slot t.
 __global__ void __launch_bounds__(kHistThreads, 1)
     hist_tiles_kernel(const float4 *__restrict__ atoms,
@@ -68,6 +114,8 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     __syncthreads();
     unsigned long long *gh = hist + (long long)sg.pair * pitch + sg.kb;
     const unsigned wl = (unsigned)sg.wl, kb = (unsigned)sg.kb;
+    const unsigned base = 0x4B000000u + kb;
+    const bool full_window = kb == 0 && wl >= nbins;
     unsigned my_oor = 0;
     for (int it_i = tk.item_begin + warp; it_i < tk.item_end;
          it_i += kHistThreads / 32) {
@@ -75,7 +123,6 @@ __global__ void __launch_bounds__(kHistThreads, 1)
       const bool diag = it.y < 0;
       const int2 TI = __ldg(&tiles[it.x]);
       const int2 TJ = __ldg(&tiles[it.y & 0x7fffffff]);
-      // row atoms lane + 32r; jlim: last column index paired with it
       float x[4], y[4], z[4];
       int jlim[4];
 #pragma unroll
@@ -89,32 +136,22 @@ __global__ void __launch_bounds__(kHistThreads, 1)
         // diag tile: pairs j <= i incl. i == j (cuDebye-v15.cu:137)
         jlim[r] = act ? (diag ? pi : 0x7fffffff) : -1;
       }
-      const f2 X01 = pk(x[0], x[1]), X23 = pk(x[2], x[3]);
-      const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
-      const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
       const float4 *bj = atoms + TJ.x;
-      const int jend = TJ.y;
-#pragma unroll 2
-      for (int j = 0; j < jend; ++j) {
-        const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
-        const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
-        int k[4];
-        bins2(X01, Y01, Z01, bx, by, bz, inv, k[0], k[1]);
-        bins2(X23, Y23, Z23, bx, by, bz, inv, k[2], k[3]);
-        unsigned old[4], lk[4];
-        bool hit[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const bool valid = j <= jlim[r];
-          lk[r] = (unsigned)k[r] - kb;
-          hit[r] = valid && lk[r] < wl;
-          my_oor += (valid && !hit[r] && (unsigned)k[r] >= nbins) ? 1u : 0u;
-          old[r] = hit[r] ? atomicAdd(&sh[lk[r] >> 1], (lk[r] & 1u) ? 0x10000u : 1u)
-                          : 0u;
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-          if (hit[r]) wrap16(old[r], lk[r], gh);
+      const bool all_valid = !diag && TI.y == kTile;  // warp-uniform
+      if (all_valid) {
+        if (full_window)
+          pair_loop<true, true>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
+                                nbins, sh, gh, my_oor);
+        else
+          pair_loop<true, false>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
+                                 nbins, sh, gh, my_oor);
+      } else {
+        if (full_window)
+          pair_loop<false, true>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
+                                 nbins, sh, gh, my_oor);
+        else
+          pair_loop<false, false>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
+                                  nbins, sh, gh, my_oor);
       }
     }
     my_oor = __reduce_add_sync(0xffffffffu, my_oor);

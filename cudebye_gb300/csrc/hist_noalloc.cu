@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int nJ = diag ? na : nb;
   unsigned long long *gh = out + kb;
   const unsigned lim = nbins - (unsigned)kb;
+  const unsigned base = 0x4B000000u + (unsigned)kb;
   unsigned my_oor = 0;
   for (;;) {
     int idx = 0;
@@ -161,17 +162,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int j = 0; j < nj; ++j) {
       const float4 b = bj[j];
       const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
-      int k[4];
-      bins2(X01, Y01, Z01, bx, by, bz, inv, k[0], k[1]);
-      bins2(X23, Y23, Z23, bx, by, bz, inv, k[2], k[3]);
       unsigned old[4], lk[4];
+      bins2(X01, Y01, Z01, bx, by, bz, inv, base, lk[0], lk[1]);
+      bins2(X23, Y23, Z23, bx, by, bz, inv, base, lk[2], lk[3]);
       bool hit[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const bool valid = j <= jlim[r];
-        lk[r] = (unsigned)k[r] - (unsigned)kb;
         hit[r] = valid && lk[r] < (unsigned)wl;
-        my_oor += (valid && !hit[r] && (unsigned)k[r] >= nbins) ? 1u : 0u;
+        my_oor += (valid && !hit[r] && lk[r] + (unsigned)kb >= nbins) ? 1u : 0u;
         old[r] = hit[r] ? atomicAdd(&sh[lk[r] >> 1], (lk[r] & 1u) ? 0x10000u : 1u)
                         : 0u;
       }

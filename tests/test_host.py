@@ -131,26 +131,41 @@ def test_xyz2deb_rmax_rule():
     assert lattice.xyz2deb_rmax(xyz) == 12
 
 
-def _exact_bin_model(p):
-    """numpy model of the kernel's roundf: t = p + 2^23 (RN even), bits,
-    tie correction; must equal roundf (half away from zero) for p >= 0."""
+def _f32_directed(x64, toward):
+    """float64 value (exact) rounded to float32 toward zero ('z') or
+    toward -inf ('d')."""
+    r = x64.astype(np.float32)
+    if toward == "z":
+        over = np.abs(r.astype(np.float64)) > np.abs(x64)
+        r[over] = np.nextafter(r[over], np.float32(0))
+    else:
+        over = r.astype(np.float64) > x64
+        r[over] = np.nextafter(r[over], np.float32(-np.inf))
+    return r
+
+
+def _kernel_round_model(p):
+    """The kernel's roundf: floor(RZ(p + 0.5)) read from the bits of
+    RD(a + 2^23) (float32 operations emulated exactly in float64)."""
     p = np.asarray(p, np.float32)
-    t = (p + np.float32(8388608.0)).astype(np.float32)
-    k = t.view(np.int32).astype(np.int64) - 0x4B000000
-    r = (t - np.float32(8388608.0)).astype(np.float32)
-    k += ((p - r).astype(np.float32) == np.float32(0.5))
-    return k
+    a = _f32_directed(p.astype(np.float64) + 0.5, "z")
+    t = _f32_directed(a.astype(np.float64) + 8388608.0, "d")
+    return t.view(np.int32).astype(np.int64) - 0x4B000000
 
 
 def test_exact_roundf_without_conversion():
     rng = np.random.default_rng(0)
     p = np.concatenate([
         rng.uniform(0, 4.2e6, 200000).astype(np.float32),
+        rng.uniform(0, 3, 100000).astype(np.float32),
         (np.arange(0, 100000, dtype=np.float32) + np.float32(0.5)),  # ties
+        np.nextafter(np.arange(1, 50000, dtype=np.float32) + np.float32(0.5),
+                     np.float32(0)),
         np.nextafter(np.float32(0.5), np.float32(0)).reshape(1),
         np.array([0, 0.5, 1.5, 2.5, 4194303.5], np.float32)])
-    want = np.floor(p.astype(np.float64) + 0.5).astype(np.int64)  # p exact in f64
-    np.testing.assert_array_equal(_exact_bin_model(p), want)
+    # roundf for p >= 0: half away from zero = floor(p + 0.5), exact in f64
+    want = np.floor(p.astype(np.float64) + 0.5).astype(np.int64)
+    np.testing.assert_array_equal(_kernel_round_model(p), want)
 
 
 def test_packed_counter_bookkeeping():
