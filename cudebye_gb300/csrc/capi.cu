@@ -82,7 +82,14 @@ void free_model(dbx_ctx *c, dbx::Model *m) {
   if (m->d_atoms) cudaFree(m->d_atoms);
   if (m->d_tiles) cudaFree(m->d_tiles);
   if (m->d_hist) cudaFree(m->d_hist);
-  c->used -= m->dev_bytes + m->hist_bytes;
+  if (m->plan_cache) {
+    for (dbx::DevBuf *b : {&m->plan_cache->lists.items, &m->plan_cache->lists.segs,
+                           &m->plan_cache->lists.tasks})
+      if (b->p) cudaFree(b->p);
+    delete m->plan_cache;
+    m->plan_cache = nullptr;
+  }
+  c->used -= m->dev_bytes + m->hist_bytes + m->plan_bytes;
 }
 
 dbx::Model *find_model(dbx_ctx *c, int64_t id) {
@@ -92,8 +99,14 @@ dbx::Model *find_model(dbx_ctx *c, int64_t id) {
 
 int64_t pitch_of(int64_t nbins) { return (nbins + 2 + 1) & ~int64_t(1); }
 
-// Histograms of all pairs, kept resident in the model.
-Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins) {
+// Histograms of all pairs, kept resident in the model. The work lists are
+// planned and uploaded once per (model, rstep, nbins) and reused. With
+// `launched` non-null the range check is left to the caller (who must call
+// hist_range_check on c->hws after the stream work it queues behind it);
+// *launched tells whether kernels were queued.
+Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
+                  bool *launched = nullptr) {
+  if (launched) *launched = false;
   if (m->d_hist && m->hist_rstep == rstep && m->hist_nbins == nbins)
     return dbx::ok();
   const int np = dbx::npairs_of(m->nspecies);
@@ -110,21 +123,40 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins) {
     m->hist_bytes = bytes;
     c->used += bytes;
   }
-  std::vector<int2> pairs;
-  for (int r = 0; r < m->nspecies; ++r)
-    for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
-  dbx::HistPlan plan;
-  DBX_TRY(dbx::hist_plan(*m, pairs, rstep, nbins, c->hist_tasks, &plan));
   size_t delta = 0;
+  if (!m->plan_cache || m->plan_rstep != rstep || m->plan_nbins != nbins) {
+    if (!m->plan_cache) m->plan_cache = new dbx::HistPlanCache();
+    std::vector<int2> pairs;
+    for (int r = 0; r < m->nspecies; ++r)
+      for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
+    m->plan_rstep = 0;
+    m->plan_nbins = 0;
+    DBX_TRY(dbx::hist_plan(*m, pairs, rstep, nbins, c->hist_tasks,
+                           &m->plan_cache->plan));
+    const size_t before = delta;
+    Error e = dbx::hist_upload(m->plan_cache->plan, &m->plan_cache->lists,
+                               c->stream, &delta);
+    m->plan_bytes += delta - before;
+    c->used += delta;
+    delta = 0;
+    if (e.code) return e;
+    c->h2d += m->plan_cache->plan.upload_bytes();
+    m->plan_rstep = rstep;
+    m->plan_nbins = nbins;
+  }
   m->hist_rstep = 0;
   m->hist_nbins = 0;
-  Error e = dbx::hist_run(*m, plan, (float)(1.0 / rstep), nbins, pitch,
-                          m->d_hist, &c->hws, c->stream, c->num_sms, &delta,
-                          &c->tm);
+  Error e = dbx::hist_launch(*m, m->plan_cache->plan, m->plan_cache->lists,
+                             &c->hws, (float)(1.0 / rstep), nbins, pitch,
+                             m->d_hist, c->stream, c->num_sms, &delta, &c->tm);
   c->used += delta;
-  c->h2d += plan.upload_bytes();
-  c->d2h += sizeof(unsigned long long);
   if (e.code != DBX_OK) return e;
+  if (launched) {
+    *launched = true;
+  } else {
+    c->d2h += sizeof(unsigned long long);
+    DBX_TRY(dbx::hist_range_check(c->hws, nbins, c->stream));
+  }
   m->hist_rstep = rstep;
   m->hist_nbins = nbins;
   m->hist_pitch = pitch;
@@ -146,7 +178,8 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   if (nq < 1) return dbx::fail(DBX_ERR_ARG, "nq must be >= 1");
   if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_FP64 && mode != DBX_DEBYE_FP32)
     return dbx::fail(DBX_ERR_ARG, "unknown Debye mode");
-  DBX_TRY(ensure_hist(c, m, rstep, nbins));
+  bool launched = false;
+  DBX_TRY(ensure_hist(c, m, rstep, nbins, &launched));
   const int np = dbx::npairs_of(m->nspecies);
   DBX_TRY(grow(c, &c->K, sizeof(double) * nq));
   DBX_TRY(grow(c, &c->ff, sizeof(double) * nq * (size_t)np));
@@ -181,6 +214,14 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
                               (const double *)c->ff.p, (double *)c->I.p,
                               c->stream));
     c->tm.stop(DBX_T_DEBYE, c->stream);
+  }
+  if (launched) {  // the histograms' range check, deferred to here
+    c->d2h += sizeof(unsigned long long);
+    Error e = dbx::hist_range_check(c->hws, nbins, c->stream);
+    if (e.code) {
+      m->hist_nbins = 0;
+      return e;
+    }
   }
   DBX_CUDA_TRY(cudaMemcpyAsync(out_I, c->I.p, sizeof(double) * nq,
                                cudaMemcpyDeviceToHost, c->stream));

@@ -85,6 +85,12 @@ struct Model {
   float4 *d_atoms = nullptr;                // natoms x (x, y, z, 0)
   int2 *d_tiles = nullptr;
   size_t dev_bytes = 0;
+  // Cached histogram plan of all pairs for (plan_rstep, plan_nbins): the
+  // work lists depend only on the geometry and the binning.
+  double plan_rstep = 0;
+  int64_t plan_nbins = 0;
+  struct HistPlanCache *plan_cache = nullptr;
+  size_t plan_bytes = 0;
   // Resident histograms (for re-scoring with new K or species).
   double hist_rstep = 0;
   int64_t hist_nbins = 0;
@@ -134,9 +140,32 @@ struct HistWorkspace {  // device-side scratch for one histogram run
   DevBuf items, segs, tasks, partial, oor;
 };
 
-// Run a plan: out = device int64 histograms [plan.nrows][pitch], zeroed
-// here; pitch >= nbins + 2 (the two bins past the end absorb the carry
-// bookkeeping of the packed counters). Returns DBX_ERR_RANGE if any pair binned at k >= nbins.
+struct HistPlanCache {  // a plan and its uploaded work lists
+  HistPlan plan;
+  HistWorkspace lists;
+};
+
+// Copy a plan's work lists (items, segments, tasks) to the device.
+Error hist_upload(const HistPlan &plan, HistWorkspace *lists,
+                  cudaStream_t stream, size_t *ws_bytes_delta);
+
+// Launch the histogram of an uploaded plan: out = device int64 histograms
+// [plan.nrows][pitch], zeroed here; pitch >= nbins + 2 (the two bins past
+// the end absorb the carry bookkeeping of the packed counters). Pairs
+// binned at k >= nbins are counted in scratch->oor on the device; read
+// them with hist_range_check. Asynchronous.
+Error hist_launch(const Model &m, const HistPlan &plan,
+                  const HistWorkspace &lists, HistWorkspace *scratch,
+                  float inv_rstep, int64_t nbins, int64_t pitch,
+                  unsigned long long *d_out, cudaStream_t stream, int num_sms,
+                  size_t *ws_bytes_delta, Timers *tm);
+
+// Wait for the stream and return DBX_ERR_RANGE if the last launch binned
+// any pair at k >= nbins.
+Error hist_range_check(const HistWorkspace &scratch, int64_t nbins,
+                       cudaStream_t stream);
+
+// hist_upload + hist_launch + hist_range_check.
 Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
                int64_t nbins, int64_t pitch, unsigned long long *d_out,
                HistWorkspace *ws, cudaStream_t stream, int num_sms,

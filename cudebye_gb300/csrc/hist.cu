@@ -322,24 +322,14 @@ static Error ensure(DevBuf *b, size_t bytes, size_t *delta) {
   return ok();
 }
 
-Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
-               int64_t nbins, int64_t pitch, unsigned long long *d_out,
-               HistWorkspace *ws, cudaStream_t stream, int num_sms,
-               size_t *ws_bytes_delta, Timers *tm) {
+Error hist_upload(const HistPlan &plan, HistWorkspace *ws, cudaStream_t stream,
+                  size_t *ws_bytes_delta) {
   const int ntasks = (int)plan.tasks.size();
   const int nsegs = (int)plan.segs.size();
-  int max_wl = 0;
-  for (const HistSeg &s : plan.segs) max_wl = std::max(max_wl, s.wl);
-  const int words = (max_wl + 1) / 2;
   DBX_TRY(ensure(&ws->items, std::max<size_t>(plan.items.size(), 1) * sizeof(int2),
                  ws_bytes_delta));
   DBX_TRY(ensure(&ws->segs, std::max(nsegs, 1) * sizeof(HistSeg), ws_bytes_delta));
   DBX_TRY(ensure(&ws->tasks, std::max(ntasks, 1) * sizeof(HistTask), ws_bytes_delta));
-  DBX_TRY(ensure(&ws->partial, std::max<size_t>((size_t)ntasks * words, 1) * 4,
-                 ws_bytes_delta));
-  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
-  DBX_CUDA_TRY(cudaMemsetAsync(
-      d_out, 0, sizeof(unsigned long long) * (size_t)pitch * plan.nrows, stream));
   if (ntasks == 0) return ok();
   DBX_CUDA_TRY(cudaMemcpyAsync(ws->items.p, plan.items.data(),
                                plan.items.size() * sizeof(int2),
@@ -350,17 +340,35 @@ Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
   DBX_CUDA_TRY(cudaMemcpyAsync(ws->tasks.p, plan.tasks.data(),
                                ntasks * sizeof(HistTask),
                                cudaMemcpyHostToDevice, stream));
+  return ok();
+}
+
+Error hist_launch(const Model &m, const HistPlan &plan,
+                  const HistWorkspace &lists, HistWorkspace *ws,
+                  float inv_rstep, int64_t nbins, int64_t pitch,
+                  unsigned long long *d_out, cudaStream_t stream, int num_sms,
+                  size_t *ws_bytes_delta, Timers *tm) {
+  const int ntasks = (int)plan.tasks.size();
+  const int nsegs = (int)plan.segs.size();
+  int max_wl = 0;
+  for (const HistSeg &s : plan.segs) max_wl = std::max(max_wl, s.wl);
+  const int words = (max_wl + 1) / 2;
+  DBX_TRY(ensure(&ws->partial, std::max<size_t>((size_t)ntasks * words, 1) * 4,
+                 ws_bytes_delta));
+  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
+  DBX_CUDA_TRY(cudaMemsetAsync(
+      d_out, 0, sizeof(unsigned long long) * (size_t)pitch * plan.nrows, stream));
   // oor counter and the task counter share one 16-byte buffer
   DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, 2 * sizeof(unsigned long long), stream));
-  const int smem = words * 4;
+  if (ntasks == 0) return ok();
   DBX_CUDA_TRY(cudaFuncSetAttribute(hist_tiles_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kHistSmemBytes));
   const int grid = std::min(ntasks, num_sms);
   tm->start(DBX_T_HIST, stream);
-  hist_tiles_kernel<<<grid, kHistThreads, smem, stream>>>(
-      m.d_atoms, m.d_tiles, (const int2 *)ws->items.p,
-      (const HistTask *)ws->tasks.p, ntasks, (const HistSeg *)ws->segs.p,
+  hist_tiles_kernel<<<grid, kHistThreads, words * 4, stream>>>(
+      m.d_atoms, m.d_tiles, (const int2 *)lists.items.p,
+      (const HistTask *)lists.tasks.p, ntasks, (const HistSeg *)lists.segs.p,
       inv_rstep, (unsigned)nbins, (unsigned *)ws->partial.p, words, d_out,
       (long long)pitch, (unsigned long long *)ws->oor.p,
       (int *)((unsigned long long *)ws->oor.p + 1));
@@ -370,13 +378,19 @@ Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
   dim3 rgrid((words + 255) / 256, nsegs);
   hist_reduce_kernel<<<rgrid, 256, 0, stream>>>((const unsigned *)ws->partial.p,
                                                 words,
-                                                (const HistSeg *)ws->segs.p,
+                                                (const HistSeg *)lists.segs.p,
                                                 d_out, (long long)pitch);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->stop(DBX_T_HIST_REDUCE, stream);
+  return ok();
+}
+
+Error hist_range_check(const HistWorkspace &ws, int64_t nbins,
+                       cudaStream_t stream) {
   unsigned long long oor = 0;
-  DBX_CUDA_TRY(cudaMemcpyAsync(&oor, ws->oor.p, sizeof(oor),
-                               cudaMemcpyDeviceToHost, stream));
+  if (ws.oor.p)
+    DBX_CUDA_TRY(cudaMemcpyAsync(&oor, ws.oor.p, sizeof(oor),
+                                 cudaMemcpyDeviceToHost, stream));
   DBX_CUDA_TRY(cudaStreamSynchronize(stream));
   if (oor)
     return fail(DBX_ERR_RANGE,
@@ -384,6 +398,16 @@ Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
                     " distances bin at or beyond rmax (nbins = " +
                     std::to_string(nbins) + "); increase rmax");
   return ok();
+}
+
+Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
+               int64_t nbins, int64_t pitch, unsigned long long *d_out,
+               HistWorkspace *ws, cudaStream_t stream, int num_sms,
+               size_t *ws_bytes_delta, Timers *tm) {
+  DBX_TRY(hist_upload(plan, ws, stream, ws_bytes_delta));
+  DBX_TRY(hist_launch(m, plan, *ws, ws, inv_rstep, nbins, pitch, d_out, stream,
+                      num_sms, ws_bytes_delta, tm));
+  return hist_range_check(*ws, nbins, stream);
 }
 
 }  // namespace dbx
