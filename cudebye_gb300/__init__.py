@@ -38,7 +38,7 @@ ERRORS = {
     -7: "DBX_ERR_RANGE", -8: "DBX_ERR_MODEL", -9: "DBX_ERR_TIMEOUT",
     -10: "DBX_ERR_IO", -11: "DBX_ERR_LIMIT",
 }
-MODES = {"tc": 0, "fp64": 1, "fp32": 2}
+MODES = {"tc": 0, "fp64": 1, "fp32": 2, "plain": 3}
 
 # Every symbol include/cudebye.h declares (checked by the CPU tests).
 EXPORTS = (
@@ -47,9 +47,10 @@ EXPORTS = (
     "dbx_pair_histogram", "dbx_histogram", "dbx_channels", "dbx_reduce_check",
     "dbx_k_grid", "dbx_atomic_prop", "dbx_intensity", "dbx_pattern",
     "dbx_set_stream", "dbx_set_timing", "dbx_get_timing", "dbx_get_traffic",
-    "dbx_run_deb", "dbx_pair_histogram_noalloc",
+    "dbx_run_deb", "dbx_pair_histogram_noalloc", "dbx_patterns",
+    "dbx_set_graphs",
 )
-TIMERS = ("hist", "hist_reduce", "prefactor", "debye")
+TIMERS = ("hist", "hist_reduce", "prefactor", "debye", "pass")
 
 
 class DebyeError(RuntimeError):
@@ -131,6 +132,11 @@ def load_library(path=None):
         "dbx_get_traffic": (ctypes.c_int, [c_p, i64p]),
         "dbx_run_deb": (ctypes.c_int, [c_p, ctypes.c_char_p, ctypes.c_char_p,
                                        ctypes.c_int]),
+        "dbx_patterns": (ctypes.c_int, [c_p, i64p, ctypes.c_int,
+                                        ctypes.c_double, i64p,
+                                        ctypes.POINTER(Species), dp,
+                                        ctypes.c_int, ctypes.c_int, dp]),
+        "dbx_set_graphs": (ctypes.c_int, [c_p, ctypes.c_int]),
         "dbx_pair_histogram_noalloc": (ctypes.c_int, [
             c_p, c_p, c_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
             ctypes.c_int64, ctypes.c_double, ctypes.c_int64, c_p, c_p]),
@@ -348,6 +354,25 @@ class Engine:
             self.ctx, model.id, rstep, nbins, sp, _ptr(K, ctypes.c_double),
             K.size, MODES[mode], _ptr(out, ctypes.c_double)))
         return out
+
+    def patterns(self, models, rstep, nbins, species, K, mode="tc", out=None):
+        """Full patterns of several resident models in one pass
+        (dbx_patterns): nbins per model, species = concatenated per-model
+        species lists (model order). Returns I[nmodels, nq]."""
+        K = np.ascontiguousarray(K, dtype=np.float64)
+        ids = np.ascontiguousarray([m.id for m in models], dtype=np.int64)
+        nb = np.ascontiguousarray(nbins, dtype=np.int64)
+        sp = (Species * len(species))(*species)
+        if out is None:
+            out = np.zeros((len(models), K.size), dtype=np.float64)
+        self._check(self.lib.dbx_patterns(
+            self.ctx, _ptr(ids, ctypes.c_int64), len(models), rstep,
+            _ptr(nb, ctypes.c_int64), sp, _ptr(K, ctypes.c_double), K.size,
+            MODES[mode], _ptr(out, ctypes.c_double)))
+        return out
+
+    def set_graphs(self, on=True):
+        self._check(self.lib.dbx_set_graphs(self.ctx, int(on)))
 
     def set_stream(self, stream_handle):
         """Launch on a caller's cudaStream_t (int handle, e.g.

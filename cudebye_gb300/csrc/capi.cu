@@ -18,6 +18,25 @@
 
 using dbx::Error;
 
+// The prepared state of the last dbx_patterns batch.
+struct BatchState {
+  std::vector<int64_t> ids, nbins;
+  std::vector<const void *> hist_ptrs;  // the models' histogram buffers
+  double rstep = 0;
+  std::vector<double> K;
+  dbx::HistPlanCache hp;
+  std::vector<int> model_col_begin;
+  std::vector<int2> col_sp;
+  int nsp = 0;
+  dbx::PrefState pref;
+  dbx::DevBuf ff, I, K_dev;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const void *> graph_ptrs;  // buffers the graph was built on
+  int tuned_tasks = 0;
+  bool valid = false;
+};
+
 struct dbx_ctx {
   int device = 0;
   int num_sms = 0;
@@ -33,6 +52,8 @@ struct dbx_ctx {
   dbx::HistWorkspace hws;
   dbx::TcState tc;
   dbx::DevBuf tmp_hist, K, ff, I;
+  BatchState batch;
+  bool graphs = true;
   std::string last_error;
 };
 
@@ -84,7 +105,7 @@ void free_model(dbx_ctx *c, dbx::Model *m) {
   if (m->d_hist) cudaFree(m->d_hist);
   if (m->plan_cache) {
     for (dbx::DevBuf *b : {&m->plan_cache->lists.items, &m->plan_cache->lists.segs,
-                           &m->plan_cache->lists.tasks})
+                           &m->plan_cache->lists.tasks, &m->plan_cache->lists.rows})
       if (b->p) cudaFree(b->p);
     delete m->plan_cache;
     m->plan_cache = nullptr;
@@ -124,15 +145,16 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
     c->used += bytes;
   }
   size_t delta = 0;
-  if (!m->plan_cache || m->plan_rstep != rstep || m->plan_nbins != nbins) {
+  if (!m->plan_cache || m->plan_rstep != rstep || m->plan_nbins != nbins ||
+      m->plan_out != m->d_hist) {
     if (!m->plan_cache) m->plan_cache = new dbx::HistPlanCache();
     std::vector<int2> pairs;
     for (int r = 0; r < m->nspecies; ++r)
       for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
     m->plan_rstep = 0;
     m->plan_nbins = 0;
-    DBX_TRY(dbx::hist_plan(*m, pairs, rstep, nbins, c->hist_tasks,
-                           &m->plan_cache->plan));
+    DBX_TRY(dbx::hist_plan(*m, pairs, rstep, nbins, m->d_hist, pitch,
+                           c->hist_tasks, &m->plan_cache->plan));
     const size_t before = delta;
     Error e = dbx::hist_upload(m->plan_cache->plan, &m->plan_cache->lists,
                                c->stream, &delta);
@@ -143,19 +165,20 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
     c->h2d += m->plan_cache->plan.upload_bytes();
     m->plan_rstep = rstep;
     m->plan_nbins = nbins;
+    m->plan_out = m->d_hist;
   }
   m->hist_rstep = 0;
   m->hist_nbins = 0;
-  Error e = dbx::hist_launch(*m, m->plan_cache->plan, m->plan_cache->lists,
-                             &c->hws, (float)(1.0 / rstep), nbins, pitch,
-                             m->d_hist, c->stream, c->num_sms, &delta, &c->tm);
+  Error e = dbx::hist_launch(m->plan_cache->plan, m->plan_cache->lists, &c->hws,
+                             (float)(1.0 / rstep), c->stream, c->num_sms,
+                             &delta, &c->tm);
   c->used += delta;
   if (e.code != DBX_OK) return e;
   if (launched) {
     *launched = true;
   } else {
     c->d2h += sizeof(unsigned long long);
-    DBX_TRY(dbx::hist_range_check(c->hws, nbins, c->stream));
+    DBX_TRY(dbx::hist_range_check(c->hws, c->stream));
   }
   m->hist_rstep = rstep;
   m->hist_nbins = nbins;
@@ -217,7 +240,7 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   }
   if (launched) {  // the histograms' range check, deferred to here
     c->d2h += sizeof(unsigned long long);
-    Error e = dbx::hist_range_check(c->hws, nbins, c->stream);
+    Error e = dbx::hist_range_check(c->hws, c->stream);
     if (e.code) {
       m->hist_nbins = 0;
       return e;
@@ -228,6 +251,248 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   c->d2h += sizeof(double) * nq;
   DBX_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return dbx::ok();
+}
+
+// Histogram buffer of model m sized for nbins (resident afterwards).
+Error alloc_hist(dbx_ctx *c, dbx::Model *m, int64_t nbins) {
+  const int np = dbx::npairs_of(m->nspecies);
+  const int64_t pitch = pitch_of(nbins);
+  const size_t bytes = sizeof(unsigned long long) * (size_t)pitch * np;
+  if (m->hist_bytes < bytes) {
+    if (m->d_hist) cudaFree(m->d_hist);
+    c->used -= m->hist_bytes;
+    m->d_hist = nullptr;
+    m->hist_bytes = 0;
+    if (c->budget && c->used + bytes > c->budget)
+      return dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by histograms");
+    DBX_CUDA_TRY(cudaMalloc(&m->d_hist, bytes));
+    m->hist_bytes = bytes;
+    c->used += bytes;
+  }
+  m->hist_pitch = pitch;
+  return dbx::ok();
+}
+
+void drop_graph(BatchState *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->graph_ptrs.clear();
+}
+
+// The device work of one batch pass: histograms, prefactors, contraction.
+Error batch_device_pass(dbx_ctx *c, dbx::Timers *tm) {
+  BatchState &b = c->batch;
+  size_t delta = 0;
+  Error e = dbx::hist_launch(b.hp.plan, b.hp.lists, &c->hws, (float)(1.0 / b.rstep),
+                             c->stream, c->num_sms, &delta, tm);
+  c->used += delta;
+  if (e.code) return e;
+  DBX_TRY(dbx::prefactor_execute(b.pref, (const double *)b.K_dev.p, (int)b.K.size(),
+                                 (double *)b.ff.p, c->stream));
+  return dbx::tc_execute(&c->tc, (const double *)b.K_dev.p, (double *)b.I.p,
+                         c->stream, tm);
+}
+
+// Time the histogram of the batch plan for a few task granularities and
+// keep the fastest (tasks per SM).
+Error autotune_tasks(dbx_ctx *c) {
+  BatchState &b = c->batch;
+  const int cand[3] = {2, 4, 8};
+  float best = 1e30f;
+  int best_t = c->hist_tasks;
+  cudaEvent_t e0, e1;
+  DBX_CUDA_TRY(cudaEventCreate(&e0));
+  DBX_CUDA_TRY(cudaEventCreate(&e1));
+  dbx::Timers off;
+  for (int t : cand) {
+    const int tasks = t * c->num_sms;
+    dbx::hist_plan_tasks(&b.hp.plan, tasks);
+    size_t delta = 0;
+    Error e = dbx::hist_upload(b.hp.plan, &b.hp.lists, c->stream, &delta);
+    c->used += delta;
+    if (e.code) return e;
+    cudaEventRecord(e0, c->stream);
+    e = dbx::hist_launch(b.hp.plan, b.hp.lists, &c->hws, (float)(1.0 / b.rstep),
+                         c->stream, c->num_sms, &delta, &off);
+    c->used += delta;
+    if (e.code) return e;
+    cudaEventRecord(e1, c->stream);
+    DBX_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      best_t = tasks;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b.tuned_tasks = best_t;
+  dbx::hist_plan_tasks(&b.hp.plan, best_t);
+  size_t delta = 0;
+  Error e = dbx::hist_upload(b.hp.plan, &b.hp.lists, c->stream, &delta);
+  c->used += delta;
+  return e;
+}
+
+Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
+                  const int64_t *ids, double rstep, const int64_t *nbins,
+                  const dbx_species *sp, const double *K, int nq, double *out_I) {
+  BatchState &b = c->batch;
+  const int nm = (int)ms.size();
+  for (int i = 0; i < nm; ++i) DBX_TRY(alloc_hist(c, ms[i], nbins[i]));
+  std::vector<const void *> hist_ptrs(nm);
+  for (int i = 0; i < nm; ++i) hist_ptrs[i] = ms[i]->d_hist;
+  const bool same = b.valid && b.rstep == rstep && b.K.size() == (size_t)nq &&
+                    b.ids == std::vector<int64_t>(ids, ids + nm) &&
+                    b.nbins == std::vector<int64_t>(nbins, nbins + nm) &&
+                    b.hist_ptrs == hist_ptrs &&
+                    std::memcmp(b.K.data(), K, sizeof(double) * nq) == 0;
+  size_t delta = 0;
+  int nsp = 0;
+  for (dbx::Model *m : ms) nsp += m->nspecies;
+  if (!same) {
+    b.valid = false;
+    drop_graph(&b);
+    b.ids.assign(ids, ids + nm);
+    b.nbins.assign(nbins, nbins + nm);
+    b.hist_ptrs = hist_ptrs;
+    b.rstep = rstep;
+    b.K.assign(K, K + nq);
+    // one plan over every (model, pair)
+    dbx::hist_plan_clear(&b.hp.plan);
+    for (int i = 0; i < nm; ++i) {
+      dbx::Model *m = ms[i];
+      std::vector<int2> pairs;
+      for (int r = 0; r < m->nspecies; ++r)
+        for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
+      DBX_TRY(dbx::hist_plan_add(*m, pairs, rstep, nbins[i], m->d_hist,
+                                 m->hist_pitch, &b.hp.plan));
+    }
+    // columns (model, pair) for the prefactor and the contraction
+    b.model_col_begin.assign(1, 0);
+    b.col_sp.clear();
+    std::vector<dbx::TcCol> cols;
+    int sp0 = 0;
+    for (int i = 0; i < nm; ++i) {
+      dbx::Model *m = ms[i];
+      const int P = m->nspecies;
+      int p = 0;
+      for (int r = 0; r < P; ++r)
+        for (int q = r; q < P; ++q, ++p) {
+          dbx::TcCol col{};
+          col.hist = m->d_hist + (size_t)p * m->hist_pitch;
+          col.nbins = nbins[i];
+          cols.push_back(col);
+          b.col_sp.push_back(make_int2(sp0 + r, sp0 + q));
+        }
+      sp0 += P;
+      b.model_col_begin.push_back((int)cols.size());
+    }
+    const int ncols = (int)cols.size();
+    DBX_TRY(grow(c, &b.K_dev, sizeof(double) * nq));
+    DBX_TRY(grow(c, &b.ff, sizeof(double) * nq * (size_t)ncols));
+    DBX_TRY(grow(c, &b.I, sizeof(double) * nq * (size_t)nm));
+    for (int i = 0; i < ncols; ++i) cols[i].ff = (const double *)b.ff.p + (size_t)i * nq;
+    DBX_CUDA_TRY(cudaMemcpyAsync(b.K_dev.p, K, sizeof(double) * nq,
+                                 cudaMemcpyHostToDevice, c->stream));
+    c->h2d += sizeof(double) * nq;
+    Error e = dbx::tc_prepare(&c->tc, cols, b.model_col_begin, rstep, K,
+                              (const double *)b.K_dev.p, nq, c->stream, &delta);
+    c->used += delta;
+    delta = 0;
+    if (e.code) return e;
+    e = dbx::hist_scratch(b.hp.plan, &c->hws, &delta);
+    c->used += delta;
+    delta = 0;
+    if (e.code) return e;
+    DBX_TRY(autotune_tasks(c));
+    DBX_TRY(dbx::hist_scratch(b.hp.plan, &c->hws, &delta));
+    c->used += delta;
+    delta = 0;
+    c->h2d += b.hp.plan.upload_bytes();
+    b.nsp = nsp;
+    b.valid = true;
+  }
+  // species may change between passes (re-scoring): upload every pass
+  Error e = dbx::prefactor_upload(&b.pref, sp, nsp, b.col_sp.data(),
+                                  (int)b.col_sp.size(), c->stream, &delta);
+  c->used += delta;
+  c->h2d += sizeof(dbx_species) * nsp + sizeof(int2) * b.col_sp.size();
+  if (e.code) return e;
+  const std::vector<const void *> ptrs = {
+      b.hp.lists.items.p, b.hp.lists.segs.p, b.hp.lists.tasks.p, b.hp.lists.rows.p,
+      c->hws.partial.p,   c->hws.oor.p,      b.pref.sp.p,        b.pref.colsp.p,
+      b.ff.p,             b.I.p,             b.K_dev.p,          c->tc.W.p,
+      c->tc.E.p,          c->tc.P.p,         c->tc.tiles.p,      c->tc.cols.p,
+      c->tc.basis.p,      c->tc.twid.p,      c->tc.nonself.p,    c->tc.err.p};
+  if (c->graphs) {
+    if (!b.exec || b.graph_ptrs != ptrs) {
+      drop_graph(&b);
+      dbx::Timers off;
+      DBX_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      Error ce = batch_device_pass(c, &off);
+      cudaGraph_t g = nullptr;
+      cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+      if (ce.code) {
+        if (g) cudaGraphDestroy(g);
+        return ce;
+      }
+      if (ee != cudaSuccess) return dbx::fail(DBX_ERR_CUDA, cudaGetErrorString(ee));
+      b.graph = g;
+      DBX_CUDA_TRY(cudaGraphInstantiate(&b.exec, g, 0));
+      b.graph_ptrs = ptrs;
+    }
+    c->tm.start(DBX_T_PASS, c->stream);
+    DBX_CUDA_TRY(cudaGraphLaunch(b.exec, c->stream));
+    c->tm.stop(DBX_T_PASS, c->stream);
+  } else {
+    DBX_TRY(batch_device_pass(c, &c->tm));
+  }
+  DBX_TRY(dbx::tc_check(&c->tc, c->stream));
+  c->d2h += sizeof(int);
+  Error re = dbx::hist_range_check(c->hws, c->stream);
+  c->d2h += sizeof(unsigned long long);
+  for (int i = 0; i < nm; ++i) {  // histograms stay resident for re-scoring
+    ms[i]->hist_rstep = re.code ? 0 : rstep;
+    ms[i]->hist_nbins = re.code ? 0 : nbins[i];
+  }
+  if (re.code) return re;
+  DBX_CUDA_TRY(cudaMemcpyAsync(out_I, b.I.p, sizeof(double) * nq * nm,
+                               cudaMemcpyDeviceToHost, c->stream));
+  c->d2h += sizeof(double) * nq * nm;
+  DBX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return dbx::ok();
+}
+
+// The plain unbatched FP32 GPU form for one model: per pair a one-thread-
+// per-pair global-atomic histogram, then the FP32 direct sum.
+Error pattern_plain(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
+                    const dbx_species *sp, const double *K, int nq,
+                    double *out_I) {
+  DBX_TRY(alloc_hist(c, m, nbins));
+  const float inv = (float)(1.0 / rstep);
+  const int P = m->nspecies;
+  int p = 0;
+  for (int r = 0; r < P; ++r)
+    for (int q = r; q < P; ++q, ++p) {
+      size_t delta = 0;
+      Error e = dbx::hist_plain(*m, r, q, inv, nbins,
+                                m->d_hist + (size_t)p * m->hist_pitch, &c->hws,
+                                c->stream, &delta);
+      c->used += delta;
+      if (e.code) return e;
+      e = dbx::hist_range_check(c->hws, c->stream);  // per pair, as the reference syncs
+      if (e.code) {
+        m->hist_nbins = 0;
+        return e;
+      }
+    }
+  m->hist_rstep = rstep;
+  m->hist_nbins = nbins;
+  return intensity(c, m, rstep, nbins, sp, K, nq, DBX_DEBYE_FP32, out_I);
 }
 
 }  // namespace
@@ -298,6 +563,13 @@ int dbx_destroy(dbx_ctx *c) {
   release(c, &c->hws.tasks);
   release(c, &c->hws.partial);
   release(c, &c->hws.oor);
+  if (c->batch.exec) cudaGraphExecDestroy(c->batch.exec);
+  if (c->batch.graph) cudaGraphDestroy(c->batch.graph);
+  for (dbx::DevBuf *b : {&c->batch.hp.lists.items, &c->batch.hp.lists.segs,
+                         &c->batch.hp.lists.tasks, &c->batch.hp.lists.rows,
+                         &c->batch.pref.sp, &c->batch.pref.colsp, &c->batch.ff,
+                         &c->batch.I, &c->batch.K_dev})
+    release(c, b);
   dbx::tc_release(&c->tc);
   release(c, &c->tmp_hist);
   release(c, &c->K);
@@ -442,18 +714,18 @@ int dbx_pair_histogram(dbx_ctx *c, int64_t id, int row, int col, double rstep,
   if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
   if (row < 0 || col < row || col >= m->nspecies)
     return set_err(c, dbx::fail(DBX_ERR_ARG, "need 0 <= row <= col < nspecies"));
-  dbx::HistPlan plan;
-  Error e = dbx::hist_plan(*m, {make_int2(row, col)}, rstep, nbins,
-                           c->hist_tasks, &plan);
-  if (e.code) return set_err(c, e);
   const int64_t pitch = pitch_of(nbins);
-  e = grow(c, &c->tmp_hist, sizeof(unsigned long long) * pitch);
+  Error e = grow(c, &c->tmp_hist, sizeof(unsigned long long) * pitch);
+  if (e.code) return set_err(c, e);
+  dbx::HistPlan plan;
+  e = dbx::hist_plan(*m, {make_int2(row, col)}, rstep, nbins,
+                     (unsigned long long *)c->tmp_hist.p, pitch, c->hist_tasks,
+                     &plan);
   if (e.code) return set_err(c, e);
   size_t delta = 0;
   c->tm.reset();
-  e = dbx::hist_run(*m, plan, (float)(1.0 / rstep), nbins, pitch,
-                    (unsigned long long *)c->tmp_hist.p, &c->hws, c->stream,
-                    c->num_sms, &delta, &c->tm);
+  e = dbx::hist_run(plan, (float)(1.0 / rstep), &c->hws, c->stream, c->num_sms,
+                    &delta, &c->tm);
   c->used += delta;
   c->h2d += plan.upload_bytes();
   c->d2h += sizeof(unsigned long long);
@@ -549,6 +821,50 @@ int dbx_pattern(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
   c->tm.reset();
   m->hist_nbins = 0;  // recompute the histograms: one full pattern
   return set_err(c, intensity(c, m, rstep, nbins, sp, K, nq, mode, out_I));
+}
+
+int dbx_set_graphs(dbx_ctx *c, int enable) {
+  if (!c) return DBX_ERR_ARG;
+  c->graphs = enable != 0;
+  return DBX_OK;
+}
+
+int dbx_patterns(dbx_ctx *c, const int64_t *ids, int nmodels, double rstep,
+                 const int64_t *nbins, const dbx_species *sp, const double *K,
+                 int nq, int mode, double *out_I) {
+  if (!c || !ids || nmodels < 1 || !nbins || !sp || !K || nq < 1 || !out_I ||
+      !(rstep > 0))
+    return DBX_ERR_ARG;
+  if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_FP64 && mode != DBX_DEBYE_FP32 &&
+      mode != DBX_PLAIN)
+    return set_err(c, dbx::fail(DBX_ERR_ARG, "unknown mode"));
+  cudaSetDevice(c->device);
+  std::vector<dbx::Model *> ms(nmodels);
+  for (int i = 0; i < nmodels; ++i) {
+    ms[i] = find_model(c, ids[i]);
+    if (!ms[i]) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
+    for (int j = 0; j < i; ++j)
+      if (ids[j] == ids[i])
+        return set_err(c, dbx::fail(DBX_ERR_ARG, "a model appears twice in a batch"));
+  }
+  c->tm.reset();
+  if (mode == DBX_DEBYE_TC)
+    return set_err(c, patterns_tc(c, ms, ids, rstep, nbins, sp, K, nq, out_I));
+  int sp0 = 0;
+  for (int i = 0; i < nmodels; ++i) {
+    Error e;
+    if (mode == DBX_PLAIN) {
+      e = pattern_plain(c, ms[i], rstep, nbins[i], sp + sp0, K, nq,
+                        out_I + (size_t)i * nq);
+    } else {
+      ms[i]->hist_nbins = 0;
+      e = intensity(c, ms[i], rstep, nbins[i], sp + sp0, K, nq, mode,
+                    out_I + (size_t)i * nq);
+    }
+    if (e.code) return set_err(c, e);
+    sp0 += ms[i]->nspecies;
+  }
+  return DBX_OK;
 }
 
 int dbx_set_stream(dbx_ctx *c, void *stream) {

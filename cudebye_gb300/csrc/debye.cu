@@ -68,6 +68,65 @@ Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
   return ok();
 }
 
+// Prefactor of many (model, pair) columns at once: column c uses species
+// col_sp[c] = {a, b} of the concatenated species array.
+__global__ void prefactor_cols_kernel(const SpeciesDev *__restrict__ sp,
+                                      const int2 *__restrict__ col_sp,
+                                      const double *__restrict__ K, int nq,
+                                      double *__restrict__ ff) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (q >= nq) return;
+  const SpeciesDev &s1 = sp[col_sp[c].x], &s2 = sp[col_sp[c].y];
+  const double rp16pi2 = -0.006332573977646;  // cuDebye-v15.cu:452
+  const double nhs = K[q] * K[q] * rp16pi2;
+  double v = s1.occ * s2.occ;
+  v = v * exp(nhs * (s1.beq + s2.beq));
+  double f1 = s1.c, f2 = s2.c;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    f1 += s1.a[i] * exp(s1.b[i] * nhs);
+    f2 += s2.a[i] * exp(s2.b[i] * nhs);
+  }
+  ff[(size_t)c * nq + q] = v * f1 * f2;
+}
+
+static Error grow_buf(DevBuf *b, size_t bytes, size_t *delta) {
+  if (b->bytes >= bytes) return ok();
+  if (b->p) {
+    cudaFree(b->p);
+    *delta -= b->bytes;
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
+  b->bytes = bytes;
+  *delta += bytes;
+  return ok();
+}
+
+Error prefactor_upload(PrefState *st, const dbx_species *sp, int nsp,
+                       const int2 *col_sp, int ncols, cudaStream_t stream,
+                       size_t *delta) {
+  DBX_TRY(grow_buf(&st->sp, sizeof(SpeciesDev) * std::max(nsp, 1), delta));
+  DBX_TRY(grow_buf(&st->colsp, sizeof(int2) * std::max(ncols, 1), delta));
+  DBX_CUDA_TRY(cudaMemcpyAsync(st->sp.p, sp, sizeof(SpeciesDev) * nsp,
+                               cudaMemcpyHostToDevice, stream));
+  DBX_CUDA_TRY(cudaMemcpyAsync(st->colsp.p, col_sp, sizeof(int2) * ncols,
+                               cudaMemcpyHostToDevice, stream));
+  st->ncols = ncols;
+  return ok();
+}
+
+Error prefactor_execute(const PrefState &st, const double *d_K, int nq,
+                        double *d_ff, cudaStream_t stream) {
+  dim3 grid((nq + 127) / 128, st.ncols);
+  prefactor_cols_kernel<<<grid, 128, 0, stream>>>(
+      (const SpeciesDev *)st.sp.p, (const int2 *)st.colsp.p, d_K, nq, d_ff);
+  DBX_CUDA_TRY(cudaGetLastError());
+  return ok();
+}
+
 constexpr int kDirectThreads = 128;
 constexpr int kDirectChunk = 128;  // bins staged per shared-memory round
 constexpr int kDirectMaxPairs = 16;

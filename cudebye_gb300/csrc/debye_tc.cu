@@ -476,10 +476,10 @@ size_t tc_bytes(const TcState *st) {
   return s;
 }
 
-Error debye_tc(TcState *st, std::vector<TcCol> cols,
-               const std::vector<int> &model_col_begin, double rstep,
-               const double *h_K, const double *d_K, int nq, double *d_I,
-               cudaStream_t stream, size_t *delta, Timers *tm) {
+Error tc_prepare(TcState *st, std::vector<TcCol> cols,
+                 const std::vector<int> &model_col_begin, double rstep,
+                 const double *h_K, const double *d_K, int nq,
+                 cudaStream_t stream, size_t *delta) {
   const int ncols = (int)cols.size();
   const int nmodels = (int)model_col_begin.size() - 1;
   if (ncols == 0 || nq < 1) return fail(DBX_ERR_ARG, "empty Debye contraction");
@@ -531,18 +531,31 @@ Error debye_tc(TcState *st, std::vector<TcCol> cols,
                                sizeof(int) * (nmodels + 1), cudaMemcpyHostToDevice,
                                stream));
   st->h2d += sizeof(TcTile) * ntiles + sizeof(TcCol) * ncols + sizeof(int) * (nmodels + 1);
-  DBX_CUDA_TRY(cudaMemsetAsync(st->nonself.p, 0, sizeof(int) * ncols, stream));
-  DBX_CUDA_TRY(cudaMemsetAsync(st->err.p, 0, sizeof(int), stream));
-  self_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>((TcCol *)st->cols.p, ncols,
-                                                       rstep);
-  const long long nwarps = (long long)ntiles * kTN;
-  weights_kernel<<<(unsigned)((nwarps * 32 + 255) / 256), 256, 0, stream>>>(
-      (const TcTile *)st->tiles.p, ntiles, (const TcCol *)st->cols.p, rstep,
-      (__nv_bfloat16 *)st->W.p, (int *)st->E.p, (int *)st->nonself.p);
-  DBX_CUDA_TRY(cudaGetLastError());
   DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kSmemBytes));
+  st->ncols = ncols;
+  st->nmodels = nmodels;
+  st->ntiles = ntiles;
+  st->nq = nq;
+  st->Qp = Qp;
+  st->rstep = rstep;
+  return ok();
+}
+
+Error tc_execute(TcState *st, const double *d_K, double *d_I,
+                 cudaStream_t stream, Timers *tm) {
+  const int ncols = st->ncols, ntiles = st->ntiles, nq = st->nq, Qp = st->Qp;
+  const int nrt = 2 * Qp / kTM;
+  DBX_CUDA_TRY(cudaMemsetAsync(st->nonself.p, 0, sizeof(int) * ncols, stream));
+  DBX_CUDA_TRY(cudaMemsetAsync(st->err.p, 0, sizeof(int), stream));
+  self_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>((TcCol *)st->cols.p, ncols,
+                                                       st->rstep);
+  const long long nwarps = (long long)ntiles * kTN;
+  weights_kernel<<<(unsigned)((nwarps * 32 + 255) / 256), 256, 0, stream>>>(
+      (const TcTile *)st->tiles.p, ntiles, (const TcCol *)st->cols.p, st->rstep,
+      (__nv_bfloat16 *)st->W.p, (int *)st->E.p, (int *)st->nonself.p);
+  DBX_CUDA_TRY(cudaGetLastError());
   tm->start(DBX_T_DEBYE, stream);
   gemm_kernel<<<nrt * ntiles, kThreads, kSmemBytes, stream>>>(
       (const __nv_bfloat16 *)st->basis.p, (const __nv_bfloat16 *)st->W.p,
@@ -550,11 +563,15 @@ Error debye_tc(TcState *st, std::vector<TcCol> cols,
       Qp, nrt, (double *)st->P.p, (int *)st->err.p);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->stop(DBX_T_DEBYE, stream);
-  dim3 rg((nq + 127) / 128, nmodels);
+  dim3 rg((nq + 127) / 128, st->nmodels);
   reduce_kernel<<<rg, 128, 0, stream>>>(
-      (const TcCol *)st->cols.p, ncols, (const int *)st->mcb.p, nmodels,
+      (const TcCol *)st->cols.p, ncols, (const int *)st->mcb.p, st->nmodels,
       (const double *)st->P.p, (const int *)st->nonself.p, d_K, nq, Qp, d_I);
   DBX_CUDA_TRY(cudaGetLastError());
+  return ok();
+}
+
+Error tc_check(TcState *st, cudaStream_t stream) {
   int herr = 0;
   DBX_CUDA_TRY(cudaMemcpyAsync(&herr, st->err.p, sizeof(int), cudaMemcpyDeviceToHost,
                                stream));
@@ -563,6 +580,16 @@ Error debye_tc(TcState *st, std::vector<TcCol> cols,
   if (herr)
     return fail(DBX_ERR_TIMEOUT, "tensor-core contraction: a bounded device wait ran out");
   return ok();
+}
+
+Error debye_tc(TcState *st, std::vector<TcCol> cols,
+               const std::vector<int> &model_col_begin, double rstep,
+               const double *h_K, const double *d_K, int nq, double *d_I,
+               cudaStream_t stream, size_t *delta, Timers *tm) {
+  DBX_TRY(tc_prepare(st, std::move(cols), model_col_begin, rstep, h_K, d_K, nq,
+                     stream, delta));
+  DBX_TRY(tc_execute(st, d_K, d_I, stream, tm));
+  return tc_check(st, stream);
 }
 
 }  // namespace dbx

@@ -24,10 +24,24 @@ struct TcState {  // cached plan data (basis, twiddles) and workspace
   double grid_rstep = 0;
   int grid_nch = 0;
   int64_t h2d = 0, d2h = 0;
+  // shape of the prepared contraction
+  int ncols = 0, nmodels = 0, ntiles = 0, nq = 0, Qp = 0;
+  double rstep = 0;
 };
 
-// I[model][q] for the columns grouped by model (model_col_begin has
+// Host part: column tiles, descriptors uploaded, basis and twiddles for a
+// new q grid. The columns are grouped by model (model_col_begin has
 // nmodels+1 offsets into cols, columns of a model in pair order).
+Error tc_prepare(TcState *st, std::vector<TcCol> cols,
+                 const std::vector<int> &model_col_begin, double rstep,
+                 const double *h_K, const double *d_K, int nq,
+                 cudaStream_t stream, size_t *bytes_delta);
+// Device part: I[model][q] (kernels and memsets only; capturable).
+Error tc_execute(TcState *st, const double *d_K, double *d_I,
+                 cudaStream_t stream, Timers *tm);
+// Wait; DBX_ERR_TIMEOUT if a bounded device wait ran out.
+Error tc_check(TcState *st, cudaStream_t stream);
+// prepare + execute + check
 Error debye_tc(TcState *st, std::vector<TcCol> cols,
                const std::vector<int> &model_col_begin, double rstep,
                const double *h_K, const double *d_K, int nq, double *d_I,

@@ -41,7 +41,7 @@ struct Timers {
   bool on = false;
   bool created = false;
   cudaEvent_t ev[DBX_NTIMERS][2];
-  bool recorded[DBX_NTIMERS] = {false, false, false, false};
+  bool recorded[DBX_NTIMERS] = {};
   void reset() {
     for (bool &r : recorded) r = false;
   }
@@ -90,6 +90,7 @@ struct Model {
   double plan_rstep = 0;
   int64_t plan_nbins = 0;
   struct HistPlanCache *plan_cache = nullptr;
+  unsigned long long *plan_out = nullptr;   // d_hist the plan writes to
   size_t plan_bytes = 0;
   // Resident histograms (for re-scoring with new K or species).
   double hist_rstep = 0;
@@ -105,39 +106,59 @@ inline int pair_index(int p, int row, int col) {
 }
 
 // ---- histogram planner + kernels (hist.cu) --------------------------------
-struct HistSeg {  // one (pair, bin window) accumulated in shared memory
-  int pair;       // output row
-  int kb;         // first bin of the window
-  int wl;         // window length in bins
+struct HistSeg {  // one (model, pair, bin window) accumulated in smem
+  const float4 *atoms;      // the model's atoms
+  const int2 *tiles;        // the model's tiles
+  unsigned long long *out;  // the pair's histogram, bin 0
+  int kb;                   // first bin of the window
+  int wl;                   // window length in bins
   int task_begin, task_end;
+  unsigned nbins;           // bins of this histogram
+  int pad;
 };
 struct HistTask {  // one CTA-sized slice of a segment's tile pairs
   int seg;
   int item_begin, item_end;
   int pad;
 };
+struct HistRow {  // an output histogram to zero before a launch
+  unsigned long long *out;
+  long long len;
+};
 
 struct HistPlan {
-  std::vector<int2> items;  // {tile I, tile J | (diag << 31)}
+  std::vector<int2> items;     // {tile I, tile J | (diag << 31)}
+  std::vector<int> item_pairs; // pairs of each item (host only)
   std::vector<HistSeg> segs;
+  std::vector<int2> seg_items; // item range of each segment (host only)
   std::vector<HistTask> tasks;
-  int window = 0;           // bins per shared-memory window
-  int nrows = 0;            // output histograms (selected pairs)
-  int64_t pairs = 0;        // binned pairs (the reference's "Distances
-                            // Expected" summed over the selected pairs)
+  std::vector<HistRow> rows;
+  int window = 0;              // largest window in bins
+  int nrows = 0;               // output histograms
+  int64_t pairs = 0;           // binned pairs (the reference's "Distances
+                               // Expected" summed over the selected pairs)
   size_t upload_bytes() const {
     return items.size() * sizeof(int2) + segs.size() * sizeof(HistSeg) +
-           tasks.size() * sizeof(HistTask);
+           tasks.size() * sizeof(HistTask) + rows.size() * sizeof(HistRow);
   }
 };
 
-// Plan the histogram of the selected pairs (list of (row, col)), cut into
-// about target_tasks CTA tasks of equal pair counts.
+// Plans: clear, add the pairs of one or more models (histogram of pairs[i]
+// written to out + i*pitch; pitch >= nbins + 2: the two bins past the end
+// absorb the carry bookkeeping of the packed counters), then split the
+// segments into about target_tasks CTA tasks of equal pair counts.
+void hist_plan_clear(HistPlan *plan);
+Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
+                    double rstep, int64_t nbins, unsigned long long *out,
+                    int64_t pitch, HistPlan *plan);
+void hist_plan_tasks(HistPlan *plan, int target_tasks);
+// clear + add + tasks for one model
 Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
-                int64_t nbins, int target_tasks, HistPlan *plan);
+                int64_t nbins, unsigned long long *out, int64_t pitch,
+                int target_tasks, HistPlan *plan);
 
-struct HistWorkspace {  // device-side scratch for one histogram run
-  DevBuf items, segs, tasks, partial, oor;
+struct HistWorkspace {  // device-side work lists and scratch
+  DevBuf items, segs, tasks, rows, partial, oor;
 };
 
 struct HistPlanCache {  // a plan and its uploaded work lists
@@ -145,35 +166,50 @@ struct HistPlanCache {  // a plan and its uploaded work lists
   HistWorkspace lists;
 };
 
-// Copy a plan's work lists (items, segments, tasks) to the device.
+// Copy a plan's work lists (items, segments, tasks, rows) to the device.
 Error hist_upload(const HistPlan &plan, HistWorkspace *lists,
                   cudaStream_t stream, size_t *ws_bytes_delta);
+// Allocate the scratch a plan needs (partial windows, counters).
+Error hist_scratch(const HistPlan &plan, HistWorkspace *scratch,
+                   size_t *ws_bytes_delta);
+// Launch the histograms of an uploaded plan: outputs zeroed, tile kernel,
+// reduce. Pairs binned at k >= nbins are counted in scratch->oor on the
+// device; read them with hist_range_check. Asynchronous; only kernels and
+// memsets, so it can be captured in a CUDA graph once hist_scratch has run.
+Error hist_launch(const HistPlan &plan, const HistWorkspace &lists,
+                  HistWorkspace *scratch, float inv_rstep, cudaStream_t stream,
+                  int num_sms, size_t *ws_bytes_delta, Timers *tm);
+// The plain form of the reference's kernels dist / dist2 (cuDebye-v15.cu:
+// 88-146): one thread per pair of the species block (row, col) of model m,
+// one global 64-bit atomicAdd per pair into out[nbins] (zeroed here).
+// Pairs at k >= nbins are counted in scratch->oor. The comparison baseline
+// of the "plain unbatched FP32 GPU form".
+Error hist_plain(const Model &m, int row, int col, float inv_rstep,
+                 int64_t nbins, unsigned long long *out, HistWorkspace *scratch,
+                 cudaStream_t stream, size_t *ws_bytes_delta);
 
-// Launch the histogram of an uploaded plan: out = device int64 histograms
-// [plan.nrows][pitch], zeroed here; pitch >= nbins + 2 (the two bins past
-// the end absorb the carry bookkeeping of the packed counters). Pairs
-// binned at k >= nbins are counted in scratch->oor on the device; read
-// them with hist_range_check. Asynchronous.
-Error hist_launch(const Model &m, const HistPlan &plan,
-                  const HistWorkspace &lists, HistWorkspace *scratch,
-                  float inv_rstep, int64_t nbins, int64_t pitch,
-                  unsigned long long *d_out, cudaStream_t stream, int num_sms,
-                  size_t *ws_bytes_delta, Timers *tm);
-
-// Wait for the stream and return DBX_ERR_RANGE if the last launch binned
-// any pair at k >= nbins.
-Error hist_range_check(const HistWorkspace &scratch, int64_t nbins,
-                       cudaStream_t stream);
-
-// hist_upload + hist_launch + hist_range_check.
-Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
-               int64_t nbins, int64_t pitch, unsigned long long *d_out,
-               HistWorkspace *ws, cudaStream_t stream, int num_sms,
-               size_t *ws_bytes_delta, Timers *tm);
+// Wait for the stream; DBX_ERR_RANGE if the last launch binned any pair at
+// k >= nbins.
+Error hist_range_check(const HistWorkspace &scratch, cudaStream_t stream);
+// upload + launch + range check
+Error hist_run(const HistPlan &plan, float inv_rstep, HistWorkspace *ws,
+               cudaStream_t stream, int num_sms, size_t *ws_bytes_delta,
+               Timers *tm);
 
 int hist_window_bins();  // shared-memory window capacity in bins
 
 // ---- Debye kernels (debye.cu) ----------------------------------------------
+struct PrefState {  // species and column descriptors of a batched prefactor
+  DevBuf sp, colsp;
+  int ncols = 0;
+};
+// Upload species (concatenated) and per-column species pairs {a, b}.
+Error prefactor_upload(PrefState *st, const dbx_species *sp, int nsp,
+                       const int2 *col_sp, int ncols, cudaStream_t stream,
+                       size_t *bytes_delta);
+// ff[c][q] for every column (kernel only; capturable).
+Error prefactor_execute(const PrefState &st, const double *d_K, int nq,
+                        double *d_ff, cudaStream_t stream);
 // out_ff[p][q] for every pair of the model's species.
 Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
                       int nq, double *d_ff, cudaStream_t stream);

@@ -87,14 +87,10 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
 // One warp = one tile pair (128 x 128 atoms). CTAs pull equal-sized tasks
 // from a global counter; task t's packed window goes to partial slot t.
 __global__ void __launch_bounds__(kHistThreads, 1)
-    hist_tiles_kernel(const float4 *__restrict__ atoms,
-                      const int2 *__restrict__ tiles,
-                      const int2 *__restrict__ items,
+    hist_tiles_kernel(const int2 *__restrict__ items,
                       const HistTask *__restrict__ tasks, int ntasks,
                       const HistSeg *__restrict__ segs, float inv,
-                      unsigned nbins, unsigned *__restrict__ partial,
-                      int words_per_task, unsigned long long *__restrict__ hist,
-                      long long pitch,
+                      unsigned *__restrict__ partial, int words_per_task,
                       unsigned long long *__restrict__ oor_total,
                       int *__restrict__ task_counter) {
   extern __shared__ unsigned sh[];
@@ -112,8 +108,11 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     for (int i = threadIdx.x; i < nw; i += kHistThreads) sh[i] = 0u;
     if (threadIdx.x == 0) s_oor = 0u;
     __syncthreads();
-    unsigned long long *gh = hist + (long long)sg.pair * pitch + sg.kb;
+    const float4 *atoms = sg.atoms;
+    const int2 *tiles = sg.tiles;
+    unsigned long long *gh = sg.out + sg.kb;
     const unsigned wl = (unsigned)sg.wl, kb = (unsigned)sg.kb;
+    const unsigned nbins = sg.nbins;
     const unsigned base = 0x4B000000u + kb;
     const bool full_window = kb == 0 && wl >= nbins;
     unsigned my_oor = 0;
@@ -171,9 +170,7 @@ __global__ void __launch_bounds__(kHistThreads, 1)
 // kernel were made earlier on the same stream.
 __global__ void hist_reduce_kernel(const unsigned *__restrict__ partial,
                                    int words_per_task,
-                                   const HistSeg *__restrict__ segs,
-                                   unsigned long long *__restrict__ hist,
-                                   long long pitch) {
+                                   const HistSeg *__restrict__ segs) {
   const HistSeg sg = segs[blockIdx.y];
   const int nw = (sg.wl + 1) >> 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw;
@@ -184,10 +181,35 @@ __global__ void hist_reduce_kernel(const unsigned *__restrict__ partial,
       lo += w & 0xFFFFu;
       hi += w >> 16;
     }
-    unsigned long long *g = hist + (long long)sg.pair * pitch + sg.kb + 2 * i;
+    unsigned long long *g = sg.out + sg.kb + 2 * i;
     g[0] += lo;
     g[1] += hi;
   }
+}
+
+// Zero the output histograms of a plan (one block per row).
+__global__ void hist_zero_kernel(const HistRow *__restrict__ rows) {
+  const HistRow r = rows[blockIdx.x];
+  for (long long i = threadIdx.x; i < r.len; i += blockDim.x) r.out[i] = 0ull;
+}
+
+// One thread per pair (i of the row block, j of the column block), blocks of
+// 16x16 pairs as in the reference's launch shape; diag keeps j <= i.
+__global__ void plain_pairs_kernel(const float4 *__restrict__ atoms, long long a0,
+                                   int na, long long b0, int nb, int diag,
+                                   float inv, unsigned nbins,
+                                   unsigned long long *__restrict__ out,
+                                   unsigned long long *__restrict__ oor) {
+  const int j = blockIdx.x * 16 + threadIdx.x;
+  const int i = blockIdx.y * 16 + threadIdx.y;
+  if (i >= na || j >= nb || (diag && j > i)) return;
+  const float4 a = atoms[a0 + i], b = atoms[b0 + j];
+  const unsigned k = bin_rel(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y),
+                             __fsub_rn(b.z, a.z), inv, 0x4B000000u);
+  if (k < nbins)
+    atomicAdd(&out[k], 1ull);
+  else
+    atomicAdd(oor, 1ull);
 }
 
 // ---------------------------------------------------------------------------
@@ -213,26 +235,34 @@ static int64_t item_pairs(int nI, int nJ, bool diag) {
   return diag ? (int64_t)nI * (nI + 1) / 2 : (int64_t)nI * nJ;
 }
 
-Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
-                int64_t nbins, int target_tasks, HistPlan *plan) {
+void hist_plan_clear(HistPlan *plan) {
+  plan->items.clear();
+  plan->item_pairs.clear();
+  plan->segs.clear();
+  plan->seg_items.clear();
+  plan->tasks.clear();
+  plan->rows.clear();
+  plan->pairs = 0;
+  plan->nrows = 0;
+  plan->window = 0;
+}
+
+Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
+                    double rstep, int64_t nbins, unsigned long long *out,
+                    int64_t pitch, HistPlan *plan) {
   if (nbins < 1 || nbins > (int64_t(1) << 22))
     return fail(DBX_ERR_ARG,
                 "histogram needs 1 <= nbins <= 4194304 (got " +
                     std::to_string(nbins) + ")");
-  plan->items.clear();
-  plan->segs.clear();
-  plan->tasks.clear();
   const int W = kWindowBins;
-  plan->window = (int)std::min<int64_t>(W, nbins);
+  plan->window = std::max(plan->window, (int)std::min<int64_t>(W, nbins));
   const int64_t nwin = (nbins + W - 1) / W;
   const double inv = 1.0 / rstep;
   std::vector<std::vector<int2>> per_win(nwin);
-  std::vector<int64_t> seg_pairs;
-  std::vector<int2> seg_items;  // item range of each segment
-  plan->pairs = 0;
-  plan->nrows = (int)pairs.size();
   for (size_t pi = 0; pi < pairs.size(); ++pi) {
     const int a = pairs[pi].x, b = pairs[pi].y;
+    unsigned long long *row = out + (int64_t)pi * pitch;
+    plan->rows.push_back(HistRow{row, pitch});
     for (auto &v : per_win) v.clear();
     for (int I = m.tile_start[a]; I < m.tile_start[a + 1]; ++I) {
       const int J0 = (a == b) ? I : m.tile_start[b];
@@ -255,56 +285,70 @@ Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
     for (int64_t w = 0; w < nwin; ++w) {
       if (per_win[w].empty()) continue;
       HistSeg s;
-      s.pair = (int)pi;
+      s.atoms = m.d_atoms;
+      s.tiles = m.d_tiles;
+      s.out = row;
       s.kb = (int)(w * W);
       s.wl = (int)std::min<int64_t>(W, nbins - w * W);
       s.task_begin = s.task_end = 0;
-      int64_t sp = 0;
+      s.nbins = (unsigned)nbins;
+      s.pad = 0;
       const int first = (int)plan->items.size();
       for (const int2 &it : per_win[w]) {
         const int2 TI = m.tiles[it.x], TJ = m.tiles[it.y & 0x7fffffff];
-        sp += item_pairs(TI.y, TJ.y, it.y < 0);
         plan->items.push_back(it);
+        plan->item_pairs.push_back((int)item_pairs(TI.y, TJ.y, it.y < 0));
       }
       plan->segs.push_back(s);
-      seg_pairs.push_back(sp);
-      seg_items.push_back(make_int2(first, (int)plan->items.size()));
+      plan->seg_items.push_back(make_int2(first, (int)plan->items.size()));
     }
     const int64_t na = m.sp_count[a], nb = m.sp_count[b];
     plan->pairs += (a == b) ? na * (na + 1) / 2 : na * nb;
+    plan->nrows += 1;
   }
+  return ok();
+}
+
+void hist_plan_tasks(HistPlan *plan, int target_tasks) {
   // Split every segment into n_s tasks of about equal pair counts, n_s
   // from the segment's share of about target_tasks tasks in all.
+  plan->tasks.clear();
+  std::vector<int64_t> seg_pairs(plan->segs.size(), 0);
   int64_t total = 0;
-  for (int64_t v : seg_pairs) total += v;
+  for (size_t s = 0; s < plan->segs.size(); ++s) {
+    for (int i = plan->seg_items[s].x; i < plan->seg_items[s].y; ++i)
+      seg_pairs[s] += plan->item_pairs[i];
+    total += seg_pairs[s];
+  }
   const double target =
       std::max(1.0, (double)total / std::max(1, target_tasks));
   for (size_t s = 0; s < plan->segs.size(); ++s) {
     HistSeg &sg = plan->segs[s];
     sg.task_begin = (int)plan->tasks.size();
-    const int i0 = seg_items[s].x, i1 = seg_items[s].y;
+    const int i0 = plan->seg_items[s].x, i1 = plan->seg_items[s].y;
     const int64_t n_s = std::max<int64_t>(
         1, std::min<int64_t>(i1 - i0, (int64_t)std::llround(seg_pairs[s] / target)));
     int64_t acc = 0, k = 1;
     int begin = i0;
     for (int i = i0; i < i1; ++i) {
-      const int2 it = plan->items[i];
-      const int2 TI = m.tiles[it.x], TJ = m.tiles[it.y & 0x7fffffff];
-      acc += item_pairs(TI.y, TJ.y, it.y < 0);
+      acc += plan->item_pairs[i];
       // close task k when the running sum reaches k/n_s of the segment
       if (i + 1 == i1 || (k < n_s && acc * n_s >= k * seg_pairs[s])) {
-        HistTask t;
-        t.seg = (int)s;
-        t.item_begin = begin;
-        t.item_end = i + 1;
-        t.pad = 0;
-        plan->tasks.push_back(t);
+        plan->tasks.push_back(HistTask{(int)s, begin, i + 1, 0});
         begin = i + 1;
         ++k;
       }
     }
     sg.task_end = (int)plan->tasks.size();
   }
+}
+
+Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
+                int64_t nbins, unsigned long long *out, int64_t pitch,
+                int target_tasks, HistPlan *plan) {
+  hist_plan_clear(plan);
+  DBX_TRY(hist_plan_add(m, pairs, rstep, nbins, out, pitch, plan));
+  hist_plan_tasks(plan, target_tasks);
   return ok();
 }
 
@@ -330,6 +374,12 @@ Error hist_upload(const HistPlan &plan, HistWorkspace *ws, cudaStream_t stream,
                  ws_bytes_delta));
   DBX_TRY(ensure(&ws->segs, std::max(nsegs, 1) * sizeof(HistSeg), ws_bytes_delta));
   DBX_TRY(ensure(&ws->tasks, std::max(ntasks, 1) * sizeof(HistTask), ws_bytes_delta));
+  DBX_TRY(ensure(&ws->rows, std::max<size_t>(plan.rows.size(), 1) * sizeof(HistRow),
+                 ws_bytes_delta));
+  if (!plan.rows.empty())
+    DBX_CUDA_TRY(cudaMemcpyAsync(ws->rows.p, plan.rows.data(),
+                                 plan.rows.size() * sizeof(HistRow),
+                                 cudaMemcpyHostToDevice, stream));
   if (ntasks == 0) return ok();
   DBX_CUDA_TRY(cudaMemcpyAsync(ws->items.p, plan.items.data(),
                                plan.items.size() * sizeof(int2),
@@ -343,34 +393,50 @@ Error hist_upload(const HistPlan &plan, HistWorkspace *ws, cudaStream_t stream,
   return ok();
 }
 
-Error hist_launch(const Model &m, const HistPlan &plan,
-                  const HistWorkspace &lists, HistWorkspace *ws,
-                  float inv_rstep, int64_t nbins, int64_t pitch,
-                  unsigned long long *d_out, cudaStream_t stream, int num_sms,
-                  size_t *ws_bytes_delta, Timers *tm) {
+Error hist_scratch(const HistPlan &plan, HistWorkspace *ws,
+                   size_t *ws_bytes_delta) {
+  int max_wl = 0;
+  for (const HistSeg &s : plan.segs) max_wl = std::max(max_wl, s.wl);
+  const int words = (max_wl + 1) / 2;
+  DBX_TRY(ensure(&ws->partial,
+                 std::max<size_t>((size_t)plan.tasks.size() * words, 1) * 4,
+                 ws_bytes_delta));
+  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
+  // The tile kernel's shared-memory opt-in, once per device (kept out of
+  // hist_launch so that a graph capture of it holds only stream work).
+  static bool attr_done[64] = {false};
+  int dev = 0;
+  DBX_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+    DBX_CUDA_TRY(cudaFuncSetAttribute(hist_tiles_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kHistSmemBytes));
+    if (dev >= 0 && dev < 64) attr_done[dev] = true;
+  }
+  return ok();
+}
+
+Error hist_launch(const HistPlan &plan, const HistWorkspace &lists,
+                  HistWorkspace *ws, float inv_rstep, cudaStream_t stream,
+                  int num_sms, size_t *ws_bytes_delta, Timers *tm) {
   const int ntasks = (int)plan.tasks.size();
   const int nsegs = (int)plan.segs.size();
   int max_wl = 0;
   for (const HistSeg &s : plan.segs) max_wl = std::max(max_wl, s.wl);
   const int words = (max_wl + 1) / 2;
-  DBX_TRY(ensure(&ws->partial, std::max<size_t>((size_t)ntasks * words, 1) * 4,
-                 ws_bytes_delta));
-  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
-  DBX_CUDA_TRY(cudaMemsetAsync(
-      d_out, 0, sizeof(unsigned long long) * (size_t)pitch * plan.nrows, stream));
+  DBX_TRY(hist_scratch(plan, ws, ws_bytes_delta));
+  if (!plan.rows.empty())
+    hist_zero_kernel<<<(unsigned)plan.rows.size(), 256, 0, stream>>>(
+        (const HistRow *)lists.rows.p);
   // oor counter and the task counter share one 16-byte buffer
   DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, 2 * sizeof(unsigned long long), stream));
   if (ntasks == 0) return ok();
-  DBX_CUDA_TRY(cudaFuncSetAttribute(hist_tiles_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kHistSmemBytes));
   const int grid = std::min(ntasks, num_sms);
   tm->start(DBX_T_HIST, stream);
   hist_tiles_kernel<<<grid, kHistThreads, words * 4, stream>>>(
-      m.d_atoms, m.d_tiles, (const int2 *)lists.items.p,
-      (const HistTask *)lists.tasks.p, ntasks, (const HistSeg *)lists.segs.p,
-      inv_rstep, (unsigned)nbins, (unsigned *)ws->partial.p, words, d_out,
-      (long long)pitch, (unsigned long long *)ws->oor.p,
+      (const int2 *)lists.items.p, (const HistTask *)lists.tasks.p, ntasks,
+      (const HistSeg *)lists.segs.p, inv_rstep, (unsigned *)ws->partial.p,
+      words, (unsigned long long *)ws->oor.p,
       (int *)((unsigned long long *)ws->oor.p + 1));
   DBX_CUDA_TRY(cudaGetLastError());
   tm->stop(DBX_T_HIST, stream);
@@ -378,36 +444,48 @@ Error hist_launch(const Model &m, const HistPlan &plan,
   dim3 rgrid((words + 255) / 256, nsegs);
   hist_reduce_kernel<<<rgrid, 256, 0, stream>>>((const unsigned *)ws->partial.p,
                                                 words,
-                                                (const HistSeg *)lists.segs.p,
-                                                d_out, (long long)pitch);
+                                                (const HistSeg *)lists.segs.p);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->stop(DBX_T_HIST_REDUCE, stream);
   return ok();
 }
 
-Error hist_range_check(const HistWorkspace &ws, int64_t nbins,
-                       cudaStream_t stream) {
+Error hist_plain(const Model &m, int row, int col, float inv_rstep,
+                 int64_t nbins, unsigned long long *out, HistWorkspace *ws,
+                 cudaStream_t stream, size_t *ws_bytes_delta) {
+  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
+  DBX_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(unsigned long long) * nbins, stream));
+  DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, 2 * sizeof(unsigned long long), stream));
+  const int na = (int)m.sp_count[row], nb = (int)m.sp_count[col];
+  if (na == 0 || nb == 0) return ok();
+  dim3 block(16, 16), grid((nb + 15) / 16, (na + 15) / 16);
+  plain_pairs_kernel<<<grid, block, 0, stream>>>(
+      m.d_atoms, m.sp_start[row], na, m.sp_start[col], nb, row == col, inv_rstep,
+      (unsigned)nbins, out, (unsigned long long *)ws->oor.p);
+  DBX_CUDA_TRY(cudaGetLastError());
+  return ok();
+}
+
+Error hist_range_check(const HistWorkspace &ws, cudaStream_t stream) {
   unsigned long long oor = 0;
   if (ws.oor.p)
     DBX_CUDA_TRY(cudaMemcpyAsync(&oor, ws.oor.p, sizeof(oor),
                                  cudaMemcpyDeviceToHost, stream));
   DBX_CUDA_TRY(cudaStreamSynchronize(stream));
   if (oor)
-    return fail(DBX_ERR_RANGE,
-                std::to_string(oor) +
-                    " distances bin at or beyond rmax (nbins = " +
-                    std::to_string(nbins) + "); increase rmax");
+    return fail(DBX_ERR_RANGE, std::to_string(oor) +
+                                   " distances bin at or beyond rmax; "
+                                   "increase rmax");
   return ok();
 }
 
-Error hist_run(const Model &m, const HistPlan &plan, float inv_rstep,
-               int64_t nbins, int64_t pitch, unsigned long long *d_out,
-               HistWorkspace *ws, cudaStream_t stream, int num_sms,
-               size_t *ws_bytes_delta, Timers *tm) {
+Error hist_run(const HistPlan &plan, float inv_rstep, HistWorkspace *ws,
+               cudaStream_t stream, int num_sms, size_t *ws_bytes_delta,
+               Timers *tm) {
   DBX_TRY(hist_upload(plan, ws, stream, ws_bytes_delta));
-  DBX_TRY(hist_launch(m, plan, *ws, ws, inv_rstep, nbins, pitch, d_out, stream,
-                      num_sms, ws_bytes_delta, tm));
-  return hist_range_check(*ws, nbins, stream);
+  DBX_TRY(hist_launch(plan, *ws, ws, inv_rstep, stream, num_sms, ws_bytes_delta,
+                      tm));
+  return hist_range_check(*ws, stream);
 }
 
 }  // namespace dbx

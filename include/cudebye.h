@@ -62,6 +62,11 @@ typedef struct dbx_species {
 #define DBX_DEBYE_FP64 1 /* FP64 CUDA-core direct sum (the reference's
                             arithmetic, debyeRowSum cuDebye-v15.cu:493-538) */
 #define DBX_DEBYE_FP32 2 /* plain FP32 direct sum (unbatched FP32 form) */
+#define DBX_PLAIN 3      /* the plain unbatched FP32 GPU form of the whole
+                            pattern: per model and pair one thread per atom
+                            pair with a global atomic (the reference's dist /
+                            dist2, cuDebye-v15.cu:88-146), then the FP32
+                            direct Debye sum; comparison baseline only */
 
 /* ---- context ---------------------------------------------------------- */
 
@@ -181,6 +186,24 @@ int dbx_pattern(dbx_ctx *ctx, int64_t model_id, double rstep, int64_t nbins,
                 const dbx_species *sp, const double *K, int nq, int mode,
                 double *out_I);
 
+/* Full patterns of many resident models in one pass: one histogram launch
+ * over every (model, pair) and one tensor-core contraction over every
+ * column, replayed as a CUDA graph while the batch (models, binning, q grid)
+ * stays the same; the histogram task granularity is autotuned on the first
+ * pass of a batch. Replaces running the reference's main() once per model
+ * (Matlab/multisim.m:19-65 runs cuDebye.exe file by file). All models share
+ * rstep and the q grid K[nq]; model i has nbins[i] bins and its species are
+ * the next nspecies(i) entries of sp (models in the order given). out_I is
+ * [nmodels][nq]. mode: DBX_DEBYE_TC (batched), DBX_DEBYE_FP64 /
+ * DBX_DEBYE_FP32 (per model, direct sums) or DBX_PLAIN (per model, the plain
+ * form). */
+int dbx_patterns(dbx_ctx *ctx, const int64_t *model_ids, int nmodels,
+                 double rstep, const int64_t *nbins, const dbx_species *sp,
+                 const double *K, int nq, int mode, double *out_I);
+
+/* CUDA-graph replay of dbx_patterns (default on). */
+int dbx_set_graphs(dbx_ctx *ctx, int enable);
+
 /* ---- streams and timing ----------------------------------------------- */
 
 /* Launch on the caller's CUDA stream (a cudaStream_t passed as void*);
@@ -196,7 +219,8 @@ int dbx_set_stream(dbx_ctx *ctx, void *cuda_stream);
 #define DBX_T_HIST_REDUCE 1 /* merge of the CTA windows */
 #define DBX_T_PREFACTOR 2   /* atomicScatter equivalent */
 #define DBX_T_DEBYE 3       /* Debye sum kernels */
-#define DBX_NTIMERS 4
+#define DBX_T_PASS 4        /* a whole dbx_patterns graph replay */
+#define DBX_NTIMERS 5
 int dbx_set_timing(dbx_ctx *ctx, int enable);
 int dbx_get_timing(const dbx_ctx *ctx, double out_ms[DBX_NTIMERS]);
 

@@ -1,0 +1,100 @@
+"""Batched patterns (dbx_patterns): many models of different sizes, species
+counts and bin counts in one histogram launch and one tensor-core
+contraction, replayed as a CUDA graph. Each model's pattern must match the
+FP64 oracle (max rel <= 1e-6) and its histograms the oracle bit for bit,
+exactly as if it ran alone."""
+import numpy as np
+import pytest
+
+import cudebye_gb300 as cd
+from cudebye_gb300 import lattice
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(seed, n=6, nmin=300, nmax=3000):
+    rng = np.random.default_rng(seed)
+    return [lattice.random_model(rng, nmin, nmax, lattice.GRID_CU, "b%d" % i, seed)
+            for i in range(n)]
+
+
+def species_of(models):
+    return [s for m in models for s in m.species]
+
+
+def check_against_oracle(engine, orc, mods, handles, I, K):
+    for m, h, row in zip(mods, handles, I):
+        hist = engine.histogram(h, m.rstep, m.nbins)  # resident after the pass
+        want_h, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins)
+        assert bad == 0
+        np.testing.assert_array_equal(hist, want_h)
+        want = orc.intensity(K, want_h, m.species, m.rstep)
+        rel = np.abs(row - want) / np.abs(want)
+        assert rel.max() <= 1e-6, (m.counts, rel.max())
+
+
+def test_batch_tc_matches_oracle_and_replays(engine, orc):
+    mods = small_batch(41)
+    tt, K = mods[0].k_grid()
+    K = K[::5]
+    handles = [engine.upload(m.xyz, m.counts) for m in mods]
+    try:
+        nb = [m.nbins for m in mods]
+        I1 = engine.patterns(handles, 1e-3, nb, species_of(mods), K)
+        check_against_oracle(engine, orc, mods, handles, I1, K)
+        # second pass: graph replay; new B factors (a re-scoring request)
+        for m in mods:
+            for s in m.species:
+                s.beq = s.beq * 0.5 + 0.1
+        I2 = engine.patterns(handles, 1e-3, nb, species_of(mods), K)
+        check_against_oracle(engine, orc, mods, handles, I2, K)
+        assert not np.array_equal(I1, I2)
+        # graphs off: the same numbers (fixed reduction order)
+        engine.set_graphs(False)
+        I3 = engine.patterns(handles, 1e-3, nb, species_of(mods), K)
+        engine.set_graphs(True)
+        np.testing.assert_array_equal(I2, I3)
+    finally:
+        for h in handles:
+            h.free()
+
+
+def test_batch_result_independent_of_batch_mates(engine):
+    """A model's pattern is the same alone and inside a batch."""
+    mods = small_batch(42, n=5)
+    tt, K = mods[0].k_grid()
+    K = K[::7]
+    handles = [engine.upload(m.xyz, m.counts) for m in mods]
+    try:
+        nb = [m.nbins for m in mods]
+        I_all = engine.patterns(handles, 1e-3, nb, species_of(mods), K)
+        for i in (0, 3):
+            I_one = engine.patterns([handles[i]], 1e-3, [nb[i]], mods[i].species, K)
+            np.testing.assert_allclose(I_one[0], I_all[i], rtol=1e-12)
+    finally:
+        for h in handles:
+            h.free()
+
+
+def test_plain_form(engine, orc):
+    mods = small_batch(43, n=3, nmax=1500)
+    tt, K = mods[0].k_grid()
+    K = K[::25]
+    handles = [engine.upload(m.xyz, m.counts) for m in mods]
+    try:
+        nb = [m.nbins for m in mods]
+        I = engine.patterns(handles, 1e-3, nb, species_of(mods), K, mode="plain")
+        for m, h, row in zip(mods, handles, I):
+            hist = engine.histogram(h, m.rstep, m.nbins)
+            want_h, _ = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins)
+            np.testing.assert_array_equal(hist, want_h)
+            want = orc.intensity(K, want_h, m.species, m.rstep)
+            assert np.abs(row - want).max() / np.abs(want).max() < 0.05
+        I64 = engine.patterns(handles, 1e-3, nb, species_of(mods), K, mode="fp64")
+        for m, h, row in zip(mods, handles, I64):
+            want_h, _ = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins)
+            want = orc.intensity(K, want_h, m.species, m.rstep)
+            np.testing.assert_allclose(row, want, rtol=1e-11)
+    finally:
+        for h in handles:
+            h.free()
