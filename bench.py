@@ -172,6 +172,63 @@ def cpu_baseline(m, K, budget_s=12.0, threads=0):
     }
 
 
+def batch_bench(eng, steps=3, seed=3, nmodels=256, check=8, plain_models=None):
+    """The batched form: 256 independent models (sc / fcc / spinel-like,
+    N log-uniform 2k-60k, 1-4 species, sigma U[0.03,0.1], B U[0.2,1.5]) on
+    the 6,001-point q grid. Patterns/s of (a) the batched engine (one
+    histogram launch + one tensor-core contraction for all 256 models,
+    CUDA-graph replay) and (b) the plain unbatched FP32 GPU form (model by
+    model: one-thread-per-pair global-atomic histogram + FP32 direct Debye
+    sum). Max relative error of (a) against the FP64 oracle on `check`
+    sampled models (every 10th q)."""
+    from cudebye_gb300 import lattice
+    from oracle import pyoracle as orc
+    mods = lattice.batch256(seed=seed, nmodels=nmodels)
+    tt, K = mods[0].k_grid()
+    sp = [s for m in mods for s in m.species]
+    nb = [m.nbins for m in mods]
+    hs = [eng.upload(m.xyz, m.counts) for m in mods]
+    pairs = sum(m.pairs for m in mods)
+    try:
+        I = eng.patterns(hs, 1e-3, nb, sp, K)  # plan, autotune, graph capture
+        I = eng.patterns(hs, 1e-3, nb, sp, K)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            I = eng.patterns(hs, 1e-3, nb, sp, K)
+        t_tc = (time.perf_counter() - t0) / steps
+        rng = np.random.default_rng(seed)
+        pick = sorted(rng.choice(len(mods), size=min(check, len(mods)),
+                                 replace=False).tolist())
+        worst = 0.0
+        for i in pick:
+            h = eng.histogram(hs[i], 1e-3, nb[i])  # resident from the pass
+            want = orc.intensity(K[::10], h, mods[i].species, 1e-3)
+            worst = max(worst, float(np.max(np.abs(I[i, ::10] - want)
+                                            / np.abs(want))))
+        # plain form over a subset (it is slow), scaled per pattern
+        sub = list(range(len(mods))) if plain_models is None else \
+            list(range(min(plain_models, len(mods))))
+        sp_sub = [s for i in sub for s in mods[i].species]
+        t0 = time.perf_counter()
+        eng.patterns([hs[i] for i in sub], 1e-3, [nb[i] for i in sub], sp_sub,
+                     K, mode="plain")
+        t_plain = (time.perf_counter() - t0) * len(mods) / len(sub)
+    finally:
+        for h in hs:
+            h.free()
+    return {
+        "models": len(mods), "binned_pairs": int(pairs),
+        "atoms_total": int(sum(m.natoms for m in mods)),
+        "patterns_per_s_batched": len(mods) / t_tc,
+        "patterns_per_s_plain": len(mods) / t_plain,
+        "speedup_batched_vs_plain": t_plain / t_tc,
+        "ms_per_batch": t_tc * 1e3,
+        "max_rel_err_vs_fp64": worst, "err_models_checked": len(pick),
+        "timing": "host wall clock around dbx_patterns (H2D species/K, graph "
+                  "replay, D2H of all intensities), mean of %d passes" % steps,
+    }
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -337,6 +394,8 @@ def run_engine(args):
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(m, K).items()
                                 if k in ("value", "unit", "cores", "kind",
                                          "sample")}
+    if not args.no_batch:
+        line["batch256"] = batch_bench(eng, plain_models=args.plain_models)
     print(json.dumps(line))
     model.free()
     eng.close()
@@ -354,6 +413,10 @@ def main():
                     help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--workload", default="spinel_10nm",
                     choices=sorted(WORKLOADS))
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 256-model batched comparison")
+    ap.add_argument("--plain-models", type=int, default=64,
+                    help="models of the batch timed in the plain form")
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = args.workload
