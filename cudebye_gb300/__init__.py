@@ -48,7 +48,8 @@ EXPORTS = (
     "dbx_k_grid", "dbx_atomic_prop", "dbx_intensity", "dbx_pattern",
     "dbx_set_stream", "dbx_set_timing", "dbx_get_timing", "dbx_get_traffic",
     "dbx_run_deb", "dbx_pair_histogram_noalloc", "dbx_patterns",
-    "dbx_set_graphs",
+    "dbx_set_graphs", "dbx_server_create", "dbx_server_submit",
+    "dbx_server_wait", "dbx_server_stats", "dbx_server_destroy",
 )
 TIMERS = ("hist", "hist_reduce", "prefactor", "debye", "pass")
 
@@ -75,6 +76,21 @@ class Species(ctypes.Structure):
             s.a[i] = float(a[i])
             s.b[i] = float(b[i])
         return s
+
+
+class Request(ctypes.Structure):
+    """dbx_request: one pattern request of the server."""
+    _fields_ = [("model", ctypes.c_int64),
+                ("x", ctypes.POINTER(ctypes.c_float)),
+                ("y", ctypes.POINTER(ctypes.c_float)),
+                ("z", ctypes.POINTER(ctypes.c_float)),
+                ("species_counts", ctypes.POINTER(ctypes.c_int64)),
+                ("nspecies", ctypes.c_int),
+                ("sp", ctypes.POINTER(Species)),
+                ("rstep", ctypes.c_double),
+                ("nbins", ctypes.c_int64),
+                ("K", ctypes.POINTER(ctypes.c_double)),
+                ("nq", ctypes.c_int)]
 
 
 _lib = None
@@ -137,6 +153,14 @@ def load_library(path=None):
                                         ctypes.POINTER(Species), dp,
                                         ctypes.c_int, ctypes.c_int, dp]),
         "dbx_set_graphs": (ctypes.c_int, [c_p, ctypes.c_int]),
+        "dbx_server_create": (ctypes.c_int, [ctypes.POINTER(c_p), ctypes.c_int,
+                                             ctypes.c_size_t]),
+        "dbx_server_submit": (ctypes.c_int, [c_p, ctypes.POINTER(Request),
+                                             i64p]),
+        "dbx_server_wait": (ctypes.c_int, [c_p, ctypes.c_int64, dp,
+                                           ctypes.c_int, i64p, dp]),
+        "dbx_server_stats": (ctypes.c_int, [c_p, i64p]),
+        "dbx_server_destroy": (ctypes.c_int, [c_p]),
         "dbx_pair_histogram_noalloc": (ctypes.c_int, [
             c_p, c_p, c_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
             ctypes.c_int64, ctypes.c_double, ctypes.c_int64, c_p, c_p]),
@@ -402,3 +426,74 @@ class Engine:
         self._check(self.lib.dbx_run_deb(
             self.ctx, path.encode(),
             out_prefix.encode() if out_prefix else None, int(verbose)))
+
+
+class Server:
+    """A pattern server (dbx_server): thread-safe submit / wait."""
+
+    def __init__(self, device=0, hbm_budget=0, lib_path=None):
+        self.lib = load_library(lib_path)
+        self.srv = ctypes.c_void_p()
+        rc = self.lib.dbx_server_create(ctypes.byref(self.srv), device,
+                                        hbm_budget)
+        if rc != DBX_OK:
+            raise DebyeError(rc, "dbx_server_create failed")
+
+    def submit(self, species, rstep, nbins, K, xyz=None, counts=None,
+               model=0):
+        """New model (xyz, counts) or re-score of a resident model id.
+        Returns a ticket."""
+        K = np.ascontiguousarray(K, dtype=np.float64)
+        sp = (Species * len(species))(*species)
+        r = Request()
+        r.model = int(model)
+        keep = [K, sp]
+        if not model:
+            xyz = np.asarray(xyz, np.float32).reshape(-1, 3)
+            cols = [np.ascontiguousarray(xyz[:, i]) for i in range(3)]
+            c = np.ascontiguousarray(counts, dtype=np.int64)
+            keep += cols + [c]
+            r.x, r.y, r.z = (_ptr(a, ctypes.c_float) for a in cols)
+            r.species_counts = _ptr(c, ctypes.c_int64)
+        r.nspecies = len(species)
+        r.sp = sp
+        r.rstep = rstep
+        r.nbins = int(nbins)
+        r.K = _ptr(K, ctypes.c_double)
+        r.nq = K.size
+        t = ctypes.c_int64()
+        rc = self.lib.dbx_server_submit(self.srv, ctypes.byref(r),
+                                        ctypes.byref(t))
+        if rc != DBX_OK:
+            raise DebyeError(rc, "submit rejected")
+        return t.value
+
+    def wait(self, ticket, nq):
+        """(I, model_id, latency_ms) of a ticket; raises on a failed request."""
+        out = np.zeros(nq, dtype=np.float64)
+        mid = ctypes.c_int64()
+        lat = ctypes.c_double()
+        rc = self.lib.dbx_server_wait(self.srv, ticket,
+                                      _ptr(out, ctypes.c_double), nq,
+                                      ctypes.byref(mid), ctypes.byref(lat))
+        if rc != DBX_OK:
+            raise DebyeError(rc, "request %d failed" % ticket)
+        return out, mid.value, lat.value
+
+    def stats(self):
+        out = np.zeros(6, np.int64)
+        self.lib.dbx_server_stats(self.srv, _ptr(out, ctypes.c_int64))
+        return dict(zip(("rounds", "completed", "resident_models",
+                         "device_bytes", "evictions", "lane_reserve"),
+                        out.tolist()))
+
+    def close(self):
+        if self.srv:
+            self.lib.dbx_server_destroy(self.srv)
+            self.srv = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

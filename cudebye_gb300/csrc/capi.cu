@@ -89,28 +89,9 @@ void release(dbx_ctx *c, dbx::DevBuf *b) {
   b->bytes = 0;
 }
 
-// Interleave the low 10 bits of v with two zero bits between each.
-uint32_t spread10(uint32_t v) {
-  v &= 0x3ffu;
-  v = (v | (v << 16)) & 0x030000FFu;
-  v = (v | (v << 8)) & 0x0300F00Fu;
-  v = (v | (v << 4)) & 0x030C30C3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
-}
-
 void free_model(dbx_ctx *c, dbx::Model *m) {
-  if (m->d_atoms) cudaFree(m->d_atoms);
-  if (m->d_tiles) cudaFree(m->d_tiles);
-  if (m->d_hist) cudaFree(m->d_hist);
-  if (m->plan_cache) {
-    for (dbx::DevBuf *b : {&m->plan_cache->lists.items, &m->plan_cache->lists.segs,
-                           &m->plan_cache->lists.tasks, &m->plan_cache->lists.rows})
-      if (b->p) cudaFree(b->p);
-    delete m->plan_cache;
-    m->plan_cache = nullptr;
-  }
-  c->used -= m->dev_bytes + m->hist_bytes + m->plan_bytes;
+  c->used -= dbx::model_device_bytes(*m);
+  dbx::model_release(m);
 }
 
 dbx::Model *find_model(dbx_ctx *c, int64_t id) {
@@ -590,101 +571,20 @@ int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
                      int64_t *model_id) {
   if (!c || !counts || nspecies < 1 || !model_id) return DBX_ERR_ARG;
   cudaSetDevice(c->device);
-  int64_t natoms = 0;
-  for (int s = 0; s < nspecies; ++s) {
-    if (counts[s] < 0) return set_err(c, dbx::fail(DBX_ERR_ARG, "negative species count"));
-    natoms += counts[s];
-  }
-  if (natoms > 0 && (!x || !y || !z))
-    return set_err(c, dbx::fail(DBX_ERR_ARG, "null coordinate array"));
-  if (natoms >= (int64_t(1) << 31))
-    return set_err(c, dbx::fail(DBX_ERR_ARG, "more than 2^31 atoms"));
   auto m = std::make_unique<dbx::Model>();
-  m->nspecies = nspecies;
-  m->natoms = natoms;
-  // Morton order on a 1024^3 grid over the model's bounding cube.
-  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  const float *xyz[3] = {x, y, z};
-  for (int64_t i = 0; i < natoms; ++i)
-    for (int d = 0; d < 3; ++d) {
-      const float v = xyz[d][i];
-      if (v < lo[d]) lo[d] = v;
-      if (v > hi[d]) hi[d] = v;
-    }
-  float ext = 0;
-  for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
-  const double scale = ext > 0 ? 1023.0 / ext : 0.0;
-  std::vector<float4> atoms(std::max<int64_t>(natoms, 1));
-  std::vector<uint32_t> code;
-  std::vector<int64_t> idx;
-  int64_t start = 0;
-  m->tile_start.push_back(0);
-  for (int s = 0; s < nspecies; ++s) {
-    const int64_t n = counts[s];
-    code.resize(n);
-    idx.resize(n);
-    for (int64_t i = 0; i < n; ++i) {
-      uint32_t q[3];
-      for (int d = 0; d < 3; ++d) {
-        double t = ((double)xyz[d][start + i] - lo[d]) * scale;
-        t = std::isfinite(t) ? std::min(std::max(t, 0.0), 1023.0) : 0.0;
-        q[d] = (uint32_t)t;
-      }
-      code[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
-      idx[i] = i;
-    }
-    std::stable_sort(idx.begin(), idx.end(),
-                     [&](int64_t a, int64_t b) { return code[a] < code[b]; });
-    for (int64_t i = 0; i < n; ++i) {
-      const int64_t src = start + idx[i];
-      atoms[start + i] = make_float4(x[src], y[src], z[src], 0.f);
-    }
-    m->sp_start.push_back(start);
-    m->sp_count.push_back(n);
-    for (int64_t t0 = 0; t0 < n; t0 += dbx::kTile) {
-      const int cnt = (int)std::min<int64_t>(dbx::kTile, n - t0);
-      m->tiles.push_back(make_int2((int)(start + t0), cnt));
-      dbx::TileBox b;
-      for (int d = 0; d < 3; ++d) {
-        b.lo[d] = INFINITY;
-        b.hi[d] = -INFINITY;
-      }
-      for (int i = 0; i < cnt; ++i) {
-        const float4 a = atoms[start + t0 + i];
-        const float v[3] = {a.x, a.y, a.z};
-        for (int d = 0; d < 3; ++d) {
-          b.lo[d] = std::min(b.lo[d], v[d]);
-          b.hi[d] = std::max(b.hi[d], v[d]);
-        }
-      }
-      m->boxes.push_back(b);
-    }
-    m->tile_start.push_back((int)m->tiles.size());
-    start += n;
-  }
-  const size_t abytes = sizeof(float4) * atoms.size();
-  const size_t tbytes = sizeof(int2) * std::max<size_t>(m->tiles.size(), 1);
-  if (c->budget && c->used + abytes + tbytes > c->budget)
+  std::vector<float4> atoms;
+  Error e = dbx::model_prepare(x, y, z, counts, nspecies, m.get(), &atoms);
+  if (e.code) return set_err(c, e);
+  const size_t need = dbx::model_upload_bytes(*m);
+  if (c->budget && c->used + need > c->budget)
     return set_err(c, dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by model"));
-  if (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
-      cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess) {
-    free_model(c, m.get());
-    return set_err(c, dbx::fail(DBX_ERR_NOMEM, "cudaMalloc failed for model"));
-  }
-  m->dev_bytes = abytes + tbytes;
-  c->used += m->dev_bytes;
-  Error e = dbx::ok();
-  if (cudaMemcpy(m->d_atoms, atoms.data(), abytes, cudaMemcpyHostToDevice) !=
-          cudaSuccess ||
-      (m->tiles.size() &&
-       cudaMemcpy(m->d_tiles, m->tiles.data(), sizeof(int2) * m->tiles.size(),
-                  cudaMemcpyHostToDevice) != cudaSuccess))
-    e = dbx::fail(DBX_ERR_CUDA, "model upload copy failed");
-  if (e.code != DBX_OK) {
-    free_model(c, m.get());
+  e = dbx::model_to_device(m.get(), atoms, c->stream);
+  if (e.code) {
+    dbx::model_release(m.get());
     return set_err(c, e);
   }
-  c->h2d += abytes + sizeof(int2) * m->tiles.size();
+  c->used += m->dev_bytes;
+  c->h2d += m->dev_bytes;
   m->id = c->next_id++;
   *model_id = m->id;
   c->models[m->id] = std::move(m);

@@ -408,7 +408,8 @@ __global__ void reduce_kernel(const TcCol *__restrict__ cols, int ncols,
                               int nmodels, const double *__restrict__ P,
                               const int *__restrict__ nonself,
                               const double *__restrict__ K, int nq, int Qp,
-                              double *__restrict__ I) {
+                              double *__restrict__ I,
+                              double *__restrict__ S_out) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int mod = blockIdx.y;
   if (q >= nq || mod >= nmodels) return;
@@ -424,9 +425,23 @@ __global__ void reduce_kernel(const TcCol *__restrict__ cols, int ncols,
       S = nonself[c] ? __longlong_as_double(0x7ff8000000000000LL) : col.self;
     else
       S = col.self + t / Kq;
+    if (S_out) S_out[(size_t)c * nq + q] = S;
     acc += S * col.ff[q];
   }
   I[(size_t)mod * nq + q] = acc;
+}
+
+// I[q] = sum over the columns of ff[c][q] * S[c][q], in column order: the
+// same arithmetic as reduce_kernel's last step, for re-scoring resident row
+// sums with new prefactors.
+__global__ void combine_kernel(const double *__restrict__ ff,
+                               const double *__restrict__ S, int ncols, int nq,
+                               double *__restrict__ I) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  double acc = 0.0;
+  for (int c = 0; c < ncols; ++c) acc += S[(size_t)c * nq + q] * ff[(size_t)c * nq + q];
+  I[q] = acc;
 }
 
 // Self-distance sum of each column: bins with r <= 0.0005 (m = n there).
@@ -566,7 +581,15 @@ Error tc_execute(TcState *st, const double *d_K, double *d_I,
   dim3 rg((nq + 127) / 128, st->nmodels);
   reduce_kernel<<<rg, 128, 0, stream>>>(
       (const TcCol *)st->cols.p, ncols, (const int *)st->mcb.p, st->nmodels,
-      (const double *)st->P.p, (const int *)st->nonself.p, d_K, nq, Qp, d_I);
+      (const double *)st->P.p, (const int *)st->nonself.p, d_K, nq, Qp, d_I,
+      st->S_out);
+  DBX_CUDA_TRY(cudaGetLastError());
+  return ok();
+}
+
+Error tc_combine(const double *d_ff, const double *d_S, int ncols, int nq,
+                 double *d_I, cudaStream_t stream) {
+  combine_kernel<<<(nq + 127) / 128, 128, 0, stream>>>(d_ff, d_S, ncols, nq, d_I);
   DBX_CUDA_TRY(cudaGetLastError());
   return ok();
 }

@@ -27,6 +27,7 @@ struct TcState {  // cached plan data (basis, twiddles) and workspace
   // shape of the prepared contraction
   int ncols = 0, nmodels = 0, ntiles = 0, nq = 0, Qp = 0;
   double rstep = 0;
+  double *S_out = nullptr;  // optional: per-column row sums S[c][q]
 };
 
 // Host part: column tiles, descriptors uploaded, basis and twiddles for a
@@ -39,6 +40,9 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
 // Device part: I[model][q] (kernels and memsets only; capturable).
 Error tc_execute(TcState *st, const double *d_K, double *d_I,
                  cudaStream_t stream, Timers *tm);
+// I[q] = sum_c ff[c][q] * S[c][q] (re-scoring resident row sums).
+Error tc_combine(const double *d_ff, const double *d_S, int ncols, int nq,
+                 double *d_I, cudaStream_t stream);
 // Wait; DBX_ERR_TIMEOUT if a bounded device wait ran out.
 Error tc_check(TcState *st, cudaStream_t stream);
 // prepare + execute + check

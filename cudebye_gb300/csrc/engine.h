@@ -100,6 +100,17 @@ struct Model {
   size_t hist_bytes = 0;
 };
 
+// Model building (model.cu): host-side sort, tiles and boxes; device copy;
+// release.
+Error model_prepare(const float *x, const float *y, const float *z,
+                    const int64_t *counts, int nspecies, Model *m,
+                    std::vector<float4> *atoms);
+size_t model_upload_bytes(const Model &m);
+Error model_to_device(Model *m, const std::vector<float4> &atoms,
+                      cudaStream_t stream);
+size_t model_device_bytes(const Model &m);  // atoms, tiles, hist, plan
+void model_release(Model *m);
+
 inline int npairs_of(int p) { return p * (p + 1) / 2; }
 inline int pair_index(int p, int row, int col) {
   return row * p - row * (row - 1) / 2 + (col - row);

@@ -1,0 +1,145 @@
+// model.cu — resident models: spatial sort, tiles and device upload.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "engine.h"
+
+namespace dbx {
+
+// Interleave the low 10 bits of v with two zero bits between each.
+static uint32_t spread10(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+Error model_prepare(const float *x, const float *y, const float *z,
+                    const int64_t *counts, int nspecies, Model *m,
+                    std::vector<float4> *atoms_out) {
+  if (!counts || nspecies < 1) return fail(DBX_ERR_ARG, "need >= 1 species");
+  int64_t natoms = 0;
+  for (int s = 0; s < nspecies; ++s) {
+    if (counts[s] < 0) return fail(DBX_ERR_ARG, "negative species count");
+    natoms += counts[s];
+  }
+  if (natoms > 0 && (!x || !y || !z)) return fail(DBX_ERR_ARG, "null coordinate array");
+  if (natoms >= (int64_t(1) << 31)) return fail(DBX_ERR_ARG, "more than 2^31 atoms");
+  m->nspecies = nspecies;
+  m->natoms = natoms;
+  // Morton order on a 1024^3 grid over the model's bounding cube, per
+  // species, then tiles of kTile atoms with their bounding boxes.
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  const float *xyz[3] = {x, y, z};
+  for (int64_t i = 0; i < natoms; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const float v = xyz[d][i];
+      if (v < lo[d]) lo[d] = v;
+      if (v > hi[d]) hi[d] = v;
+    }
+  float ext = 0;
+  for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
+  const double scale = ext > 0 ? 1023.0 / ext : 0.0;
+  std::vector<float4> &atoms = *atoms_out;
+  atoms.assign(std::max<int64_t>(natoms, 1), make_float4(0, 0, 0, 0));
+  std::vector<uint64_t> key;
+  int64_t start = 0;
+  m->tile_start.assign(1, 0);
+  m->tiles.clear();
+  m->boxes.clear();
+  m->sp_start.clear();
+  m->sp_count.clear();
+  for (int s = 0; s < nspecies; ++s) {
+    const int64_t n = counts[s];
+    // (code << 32 | index): one sort gives a stable Morton order
+    key.resize(n);
+    for (int64_t i = 0; i < n; ++i) {
+      uint32_t q[3];
+      for (int d = 0; d < 3; ++d) {
+        double t = ((double)xyz[d][start + i] - lo[d]) * scale;
+        t = std::isfinite(t) ? std::min(std::max(t, 0.0), 1023.0) : 0.0;
+        q[d] = (uint32_t)t;
+      }
+      const uint64_t code = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+      key[i] = (code << 32) | (uint64_t)i;
+    }
+    std::sort(key.begin(), key.end());
+    for (int64_t i = 0; i < n; ++i) {
+      const int64_t src = start + (int64_t)(key[i] & 0xffffffffu);
+      atoms[start + i] = make_float4(x[src], y[src], z[src], 0.f);
+    }
+    m->sp_start.push_back(start);
+    m->sp_count.push_back(n);
+    for (int64_t t0 = 0; t0 < n; t0 += kTile) {
+      const int cnt = (int)std::min<int64_t>(kTile, n - t0);
+      m->tiles.push_back(make_int2((int)(start + t0), cnt));
+      TileBox b;
+      for (int d = 0; d < 3; ++d) {
+        b.lo[d] = INFINITY;
+        b.hi[d] = -INFINITY;
+      }
+      for (int i = 0; i < cnt; ++i) {
+        const float4 a = atoms[start + t0 + i];
+        const float v[3] = {a.x, a.y, a.z};
+        for (int d = 0; d < 3; ++d) {
+          b.lo[d] = std::min(b.lo[d], v[d]);
+          b.hi[d] = std::max(b.hi[d], v[d]);
+        }
+      }
+      m->boxes.push_back(b);
+    }
+    m->tile_start.push_back((int)m->tiles.size());
+    start += n;
+  }
+  return ok();
+}
+
+size_t model_upload_bytes(const Model &m) {
+  return sizeof(float4) * std::max<int64_t>(m.natoms, 1) +
+         sizeof(int2) * std::max<size_t>(m.tiles.size(), 1);
+}
+
+Error model_to_device(Model *m, const std::vector<float4> &atoms,
+                      cudaStream_t stream) {
+  const size_t abytes = sizeof(float4) * atoms.size();
+  const size_t tbytes = sizeof(int2) * std::max<size_t>(m->tiles.size(), 1);
+  if (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
+      cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess)
+    return fail(DBX_ERR_NOMEM, "cudaMalloc failed for model");
+  m->dev_bytes = abytes + tbytes;
+  DBX_CUDA_TRY(cudaMemcpyAsync(m->d_atoms, atoms.data(), abytes,
+                               cudaMemcpyHostToDevice, stream));
+  if (!m->tiles.empty())
+    DBX_CUDA_TRY(cudaMemcpyAsync(m->d_tiles, m->tiles.data(),
+                                 sizeof(int2) * m->tiles.size(),
+                                 cudaMemcpyHostToDevice, stream));
+  return ok();
+}
+
+size_t model_device_bytes(const Model &m) {
+  return m.dev_bytes + m.hist_bytes + m.plan_bytes;
+}
+
+void model_release(Model *m) {
+  if (m->d_atoms) cudaFree(m->d_atoms);
+  if (m->d_tiles) cudaFree(m->d_tiles);
+  if (m->d_hist) cudaFree(m->d_hist);
+  if (m->plan_cache) {
+    for (DevBuf *b : {&m->plan_cache->lists.items, &m->plan_cache->lists.segs,
+                      &m->plan_cache->lists.tasks, &m->plan_cache->lists.rows})
+      if (b->p) cudaFree(b->p);
+    delete m->plan_cache;
+    m->plan_cache = nullptr;
+  }
+  m->d_atoms = nullptr;
+  m->d_tiles = nullptr;
+  m->d_hist = nullptr;
+  m->dev_bytes = m->hist_bytes = m->plan_bytes = 0;
+}
+
+}  // namespace dbx

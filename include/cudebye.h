@@ -228,6 +228,47 @@ int dbx_get_timing(const dbx_ctx *ctx, double out_ms[DBX_NTIMERS]);
  * out[0] host to device, out[1] device to host. */
 int dbx_get_traffic(const dbx_ctx *ctx, int64_t out[2]);
 
+/* ---- serving ---------------------------------------------------------- */
+
+/* A pattern server on one GPU: a worker thread admits pattern requests by
+ * HBM footprint (idle resident models evicted least recently used first),
+ * serves all admitted requests of a round together (the histograms of all
+ * new models in one launch, then per request the contraction or, for new
+ * species parameters on the same q grid, a weighted sum of the resident
+ * per-pair row sums), and overlaps two rounds on two streams so requests
+ * that arrive while others run are admitted as soon as a lane and memory
+ * free up. No counterpart in the reference (one pattern per process run;
+ * Matlab/multisim.m:19-65 loops over files). Thread-safe: any host thread
+ * may submit and wait. */
+typedef struct dbx_server dbx_server;
+
+typedef struct dbx_request {
+  int64_t model;                 /* 0: new model from x/y/z/species_counts;
+                                    else a resident model returned by an
+                                    earlier request (re-scoring) */
+  const float *x, *y, *z;        /* new model: FP32 coordinates grouped by
+                                    species */
+  const int64_t *species_counts; /* new model: atoms per species */
+  int nspecies;                  /* entries of sp (and species_counts) */
+  const dbx_species *sp;         /* species parameters of this request */
+  double rstep;                  /* bin width; re-scores repeat the model's */
+  int64_t nbins;                 /* bins; re-scores repeat the model's */
+  const double *K;               /* q grid of this request */
+  int nq;
+} dbx_request;
+
+int dbx_server_create(dbx_server **srv, int device, size_t hbm_budget_bytes);
+/* Copies the request and returns at once with a ticket. */
+int dbx_server_submit(dbx_server *srv, const dbx_request *req, int64_t *ticket);
+/* Blocks until the ticket's pattern is done: out_I[nq] (nq >= the request's
+ * nq), the model id to re-score it later, and submit-to-done latency. */
+int dbx_server_wait(dbx_server *srv, int64_t ticket, double *out_I, int nq,
+                    int64_t *model_out, double *latency_ms);
+/* out = {rounds, completed requests, resident models, device bytes held
+ * (models and lane workspaces), evictions, bytes kept free for the lanes}. */
+int dbx_server_stats(dbx_server *srv, int64_t out[6]);
+int dbx_server_destroy(dbx_server *srv);
+
 /* ---- whole-file drop-in ----------------------------------------------- */
 
 /* The reference's main() (cuDebye-v15.cu:599-1004) on the GPU: read
