@@ -229,6 +229,83 @@ def batch_bench(eng, steps=3, seed=3, nmodels=256, check=8, plain_models=None):
     }
 
 
+def serving_bench(rates=(5, 20, 50, 100, 200), seconds=6.0, pool=32, seed=4):
+    """The serving form: Poisson arrivals at each rate for `seconds`; each
+    request is a spherical lattice model of 1,000-200,000 atoms
+    (log-uniform, 1-4 species) with its own 2theta grid of 2,000-20,000
+    points, or, with probability 0.2, a re-scoring of a resident model with
+    new B factors. Latency = submit to result, measured by the server.
+    Requests are drawn from a pool of `pool` seeded models (generated once)."""
+    import concurrent.futures as cf
+    import cudebye_gb300 as cd
+    from cudebye_gb300 import lattice
+    rng = np.random.default_rng(seed)
+    models = [lattice.serving_request(rng) for _ in range(pool)]
+    grids = [m.k_grid()[1] for m in models]
+    out = []
+    with cd.Server(0) as srv:
+        # warm-up: one pass over a few pool models
+        for m, K in list(zip(models, grids))[:4]:
+            srv.wait(srv.submit(m.species, m.rstep, m.nbins, K, xyz=m.xyz,
+                                counts=m.counts), len(K))
+        for rate in rates:
+            lat, done_t, resident = [], [], []
+            lock = threading.Lock()
+            ex = cf.ThreadPoolExecutor(max_workers=64)
+
+            def waiter(t, nq, pi, t0):
+                I, mid, ms = srv.wait(t, nq)
+                with lock:
+                    lat.append(ms)
+                    done_t.append(time.perf_counter() - t0)
+                    if pi is not None:
+                        resident.append((mid, pi))
+
+            t0 = time.perf_counter()
+            tnext, k, futs, nsub, nres = 0.0, 0, [], 0, 0
+            while tnext < seconds:
+                now = time.perf_counter() - t0
+                if now < tnext:
+                    time.sleep(min(tnext - now, 0.002))
+                    continue
+                with lock:
+                    can = bool(resident)
+                if can and rng.random() < 0.2:
+                    with lock:
+                        mid, pi = resident[int(rng.integers(len(resident)))]
+                    m = models[pi]
+                    sp = [lattice.species(n, s.occ, float(rng.uniform(0.2, 1.5)))
+                          for n, s in zip(m.names, m.species)]
+                    t = srv.submit(sp, m.rstep, m.nbins, grids[pi], model=mid)
+                    futs.append(ex.submit(waiter, t, len(grids[pi]), None, t0))
+                    nres += 1
+                else:
+                    pi = k % pool
+                    k += 1
+                    m = models[pi]
+                    t = srv.submit(m.species, m.rstep, m.nbins, grids[pi],
+                                   xyz=m.xyz, counts=m.counts)
+                    futs.append(ex.submit(waiter, t, len(grids[pi]), pi, t0))
+                nsub += 1
+                tnext += rng.exponential(1.0 / rate)
+            for f in futs:
+                f.result()
+            ex.shutdown()
+            span = max(done_t) if done_t else seconds
+            out.append({"rate": rate, "submitted": nsub, "rescored": nres,
+                        "patterns_per_s": len(lat) / span,
+                        "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99))})
+        st = srv.stats()
+    sat = max([o["rate"] for o in out
+               if o["patterns_per_s"] >= 0.9 * o["rate"]] or [0])
+    return {"rates": out, "saturation_req_per_s": sat,
+            "seconds_per_rate": seconds, "pool_models": pool,
+            "rounds": st["rounds"], "evictions": st["evictions"],
+            "timing": "host clock; latency measured by the server from "
+                      "submit to result (incl. upload, queueing, readback)"}
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -396,9 +473,11 @@ def run_engine(args):
                                          "sample")}
     if not args.no_batch:
         line["batch256"] = batch_bench(eng, plain_models=args.plain_models)
-    print(json.dumps(line))
     model.free()
     eng.close()
+    if not args.no_serve:
+        line["serving"] = serving_bench(seconds=args.serve_seconds)
+    print(json.dumps(line))
     return 0
 
 
@@ -417,6 +496,10 @@ def main():
                     help="skip the 256-model batched comparison")
     ap.add_argument("--plain-models", type=int, default=64,
                     help="models of the batch timed in the plain form")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="skip the serving run")
+    ap.add_argument("--serve-seconds", type=float, default=6.0,
+                    help="seconds of Poisson arrivals per rate")
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = args.workload
