@@ -28,7 +28,9 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_build", "libcudebye.so")
+# CUDEBYE_LIB names another build of the library (e.g. an installed copy).
+LIB_PATH = os.environ.get("CUDEBYE_LIB") or os.path.join(_HERE, "_build",
+                                                         "libcudebye.so")
 CLI_PATH = os.path.join(_HERE, "_build", "cudebye")
 
 DBX_OK = 0
@@ -50,6 +52,7 @@ EXPORTS = (
     "dbx_run_deb", "dbx_pair_histogram_noalloc", "dbx_patterns",
     "dbx_set_graphs", "dbx_server_create", "dbx_server_submit",
     "dbx_server_wait", "dbx_server_stats", "dbx_server_destroy",
+    "dbx_check_sqrt",
 )
 TIMERS = ("hist", "hist_reduce", "prefactor", "debye", "pass")
 
@@ -153,6 +156,8 @@ def load_library(path=None):
                                         ctypes.POINTER(Species), dp,
                                         ctypes.c_int, ctypes.c_int, dp]),
         "dbx_set_graphs": (ctypes.c_int, [c_p, ctypes.c_int]),
+        "dbx_check_sqrt": (ctypes.c_int, [c_p, ctypes.c_uint32, ctypes.c_uint32,
+                                          i64p]),
         "dbx_server_create": (ctypes.c_int, [ctypes.POINTER(c_p), ctypes.c_int,
                                              ctypes.c_size_t]),
         "dbx_server_submit": (ctypes.c_int, [c_p, ctypes.POINTER(Request),
@@ -394,6 +399,15 @@ class Engine:
             _ptr(nb, ctypes.c_int64), sp, _ptr(K, ctypes.c_double), K.size,
             MODES[mode], _ptr(out, ctypes.c_double)))
         return out
+
+    def check_sqrt(self, lo_bits=0, hi_bits=0x7F800000):
+        """Device check of the histogram kernels' square root against the
+        IEEE one over the floats with bits in [lo_bits, hi_bits]:
+        (checked, mismatches, smallest mismatching bits or -1)."""
+        out = np.zeros(3, np.int64)
+        self._check(self.lib.dbx_check_sqrt(self.ctx, lo_bits, hi_bits,
+                                            _ptr(out, ctypes.c_int64)))
+        return int(out[0]), int(out[1]), int(out[2])
 
     def set_graphs(self, on=True):
         self._check(self.lib.dbx_set_graphs(self.ctx, int(on)))

@@ -647,6 +647,13 @@ int dbx_histogram(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
                               dbx::npairs_of(m->nspecies), out));
 }
 
+int dbx_check_sqrt(dbx_ctx *c, uint32_t lo_bits, uint32_t hi_bits,
+                   int64_t out[3]) {
+  if (!c || !out) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  return set_err(c, dbx::check_sqrt(lo_bits, hi_bits, c->num_sms, c->stream, out));
+}
+
 int dbx_reduce_check(const int64_t *counts, int64_t nbins, double rstep,
                      int64_t n_row, int64_t n_col, int diag, int64_t out[4]) {
   if (!counts || !out || nbins < 1) return DBX_ERR_ARG;

@@ -208,6 +208,9 @@ Error hist_run(const HistPlan &plan, float inv_rstep, HistWorkspace *ws,
                Timers *tm);
 
 int hist_window_bins();  // shared-memory window capacity in bins
+// Device check of the histogram kernels' square root (dbx_check_sqrt).
+Error check_sqrt(unsigned lo, unsigned hi, int num_sms, cudaStream_t stream,
+                 int64_t out[3]);
 
 // ---- Debye kernels (debye.cu) ----------------------------------------------
 struct PrefState {  // species and column descriptors of a batched prefactor

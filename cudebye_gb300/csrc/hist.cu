@@ -30,56 +30,108 @@
 namespace dbx {
 
 constexpr int kHistThreads = 1024;
-// Dynamic shared memory per CTA for the window (bytes); 1 CTA per SM.
-constexpr int kHistSmemBytes = 224 * 1024;
-constexpr int kWindowBins = (kHistSmemBytes / 4) * 2;  // 114688, even
+// Dynamic shared memory per CTA: the window (224 KB of packed counters) and
+// 64 lane-private spare words; 1 CTA per SM.
+constexpr int kWindowBins = (224 * 1024 / 4) * 2;  // 114688, even
+constexpr int kSpareWords = 64;
+constexpr int kHistSmemBytes = (kWindowBins / 2 + kSpareWords) * 4;
 
 int hist_window_bins() { return kWindowBins; }
+
+// Wrap compensation of one add whose 16-bit half went from 0xFFFF to 0.
+// v is the add's virtual bin: v < wl a bin of the window; wl <= v < vend a
+// half of an out-of-range counter (the spare words after the window, and
+// bin wl itself when wl is odd); v >= vend an ignore word (not counted).
+// The count of virtual bin v is its stored half + 65536 per wrap - 1 per
+// carry received from the low half of its word; compensations of bins go
+// to the global histogram, those of out-of-range counters to oor_total.
+__device__ __forceinline__ void wrap_fix(unsigned old, unsigned v, unsigned wl,
+                                         unsigned vend,
+                                         unsigned long long *gh,
+                                         unsigned long long *oor_total) {
+  if (v >= vend) return;
+  atomicAdd(v < wl ? &gh[v] : oor_total, 65536ull);
+  if ((v & 1u) == 0u) {  // a low half carried 1 into the high half (v + 1)
+    unsigned long long *hi = v + 1 < wl ? &gh[v + 1] : oor_total;
+    atomicAdd(hi, ~0ull);
+    if ((old >> 16) == 0xFFFFu) atomicAdd(hi, 65536ull);
+  }
+}
 
 // The column-atom loop of one tile pair for one warp: lanes hold four row
 // atoms; each column atom is one warp-uniform 16-byte load serving four
 // pairs. kAllValid: a full 128 x 128 off-diagonal tile pair (no per-pair
 // validity test). kFullWindow: the window covers bins [0, nbins), so a
 // valid pair that misses it is out of range.
+//
+// Every pair makes exactly one shared atomic, with no branch: its virtual
+// bin e is the window bin when it hits, else this lane's out-of-range
+// counter vo (a valid pair beyond the histogram) or ignore word vi (a pair
+// outside a diagonal or partial tile, or in another window). Lane-private
+// spare words avoid same-address serialisation; adds to ignore words are
+// 0. Bins are carried as the raw bits of the rounding float, u = e + base
+// (base even, so u and e have the same parity), and the window's shared
+// address is pre-offset by base: word address = sadj + 4 (u >> 1). Whether
+// an add wrapped its half is read from the returned old value; one test of
+// the four old words' sign bits guards the rare compensation.
 template <bool kAllValid, bool kFullWindow>
 __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
                                           int jend, const float (&x)[4],
                                           const float (&y)[4],
                                           const float (&z)[4],
                                           const int (&jlim)[4], float inv,
-                                          unsigned base, unsigned wl,
-                                          unsigned kb, unsigned nbins,
-                                          unsigned *sh, unsigned long long *gh,
-                                          unsigned &my_oor) {
+                                          unsigned base, unsigned sadj,
+                                          unsigned wl, unsigned kb,
+                                          unsigned nbins,
+                                          unsigned long long *gh,
+                                          unsigned vo, unsigned vi,
+                                          unsigned vend,
+                                          unsigned long long *oor_total) {
   const f2 X01 = pk(x[0], x[1]), X23 = pk(x[2], x[3]);
   const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
   const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
+  const unsigned uo = vo + base, ui = vi + base;
 #pragma unroll 2
   for (int j = 0; j < jend; ++j) {
     const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
     const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
-    unsigned lk[4], old[4];
-    bins2(X01, Y01, Z01, bx, by, bz, inv, base, lk[0], lk[1]);
-    bins2(X23, Y23, Z23, bx, by, bz, inv, base, lk[2], lk[3]);
-    bool hit[4];
+    unsigned u[4], old[4];
+    bins2(X01, Y01, Z01, bx, by, bz, inv, 0u, u[0], u[1]);
+    bins2(X23, Y23, Z23, bx, by, bz, inv, 0u, u[2], u[3]);
+    unsigned any = 0u;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const bool valid = kAllValid || j <= jlim[r];
-      hit[r] = valid && lk[r] < wl;
-      if (kFullWindow)
-        my_oor += (valid && !hit[r]) ? 1u : 0u;
-      else
-        my_oor += (valid && !hit[r] && lk[r] + kb >= nbins) ? 1u : 0u;
-      old[r] = hit[r] ? atomicAdd(&sh[lk[r] >> 1], (lk[r] & 1u) ? 0x10000u : 1u)
-                      : 0u;
+      bool ignore = false;
+      if (kFullWindow) {
+        // bins >= wl all count as out of range: clamp them to vo
+        u[r] = valid ? min(u[r], uo) : ui;
+        ignore = !valid;
+      } else {
+        const unsigned lk = u[r] - base;
+        const bool oor = valid && lk + kb >= nbins;
+        const bool hit = valid && lk < wl;
+        u[r] = hit ? u[r] : (oor ? uo : ui);
+        ignore = !hit && !oor;
+      }
+      // 1 << (16 * (u & 1)): the shift count is taken mod 32
+      unsigned inc = __funnelshift_l(0u, 1u, u[r] << 4);
+      if (ignore) inc = 0u;  // ignore words stay 0
+      asm volatile("atom.shared.add.u32 %0, [%1], %2;"
+                   : "=r"(old[r])
+                   : "r"(sadj + ((u[r] >> 1) << 2)), "r"(inc));
+      any |= old[r];
     }
-    bool w[4];
+    // A wrap returns a half at 0xFFFF, so its bit 15 is set: the filter
+    // passes only when some counter of these words has reached 32768.
+    if (any & 0x80008000u) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) w[r] = hit[r] && wrapped16(old[r], lk[r]);
-    if (w[0] | w[1] | w[2] | w[3]) {
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-        if (w[r]) wrap16(old[r], lk[r], gh);
+      for (int r = 0; r < 4; ++r) {
+        // rotate the added half to the top (by 16 for an even bin)
+        const unsigned rot = u[r] * 16u + 16u;
+        if (__funnelshift_l(old[r], old[r], rot) >= 0xFFFF0000u)
+          wrap_fix(old[r], u[r] - base, wl, vend, gh, oor_total);
+      }
     }
   }
 }
@@ -94,7 +146,6 @@ __global__ void __launch_bounds__(kHistThreads, 1)
                       unsigned long long *__restrict__ oor_total,
                       int *__restrict__ task_counter) {
   extern __shared__ unsigned sh[];
-  __shared__ unsigned s_oor;
   __shared__ int s_task;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (;;) {
@@ -105,9 +156,16 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     const HistTask tk = tasks[t];
     const HistSeg sg = segs[tk.seg];
     const int nw = (sg.wl + 1) >> 1;
-    for (int i = threadIdx.x; i < nw; i += kHistThreads) sh[i] = 0u;
-    if (threadIdx.x == 0) s_oor = 0u;
+    // window words, then 32 out-of-range words and 32 ignore words (one
+    // each per lane), addressed as virtual bins 2 * word
+    for (int i = threadIdx.x; i < nw + kSpareWords; i += kHistThreads)
+      sh[i] = 0u;
     __syncthreads();
+    const unsigned vo = 2u * ((unsigned)nw + lane), vi = vo + 64u;
+    const unsigned vend = 2u * ((unsigned)nw + 32u);
+    // shared address of word 0 minus 4 (base >> 1), mod 2^32
+    const unsigned sadj = (unsigned)__cvta_generic_to_shared(sh) -
+                          ((0x4B000000u + (unsigned)sg.kb) >> 1) * 4u;
     const float4 *atoms = sg.atoms;
     const int2 *tiles = sg.tiles;
     unsigned long long *gh = sg.out + sg.kb;
@@ -115,7 +173,6 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     const unsigned nbins = sg.nbins;
     const unsigned base = 0x4B000000u + kb;
     const bool full_window = kb == 0 && wl >= nbins;
-    unsigned my_oor = 0;
     for (int it_i = tk.item_begin + warp; it_i < tk.item_end;
          it_i += kHistThreads / 32) {
       const int2 it = __ldg(&items[it_i]);
@@ -139,27 +196,30 @@ __global__ void __launch_bounds__(kHistThreads, 1)
       const bool all_valid = !diag && TI.y == kTile;  // warp-uniform
       if (all_valid) {
         if (full_window)
-          pair_loop<true, true>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
-                                nbins, sh, gh, my_oor);
+          pair_loop<true, true>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
+                                nbins, gh, vo, vi, vend, oor_total);
         else
-          pair_loop<true, false>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
-                                 nbins, sh, gh, my_oor);
+          pair_loop<true, false>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
+                                 nbins, gh, vo, vi, vend, oor_total);
       } else {
         if (full_window)
-          pair_loop<false, true>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
-                                 nbins, sh, gh, my_oor);
+          pair_loop<false, true>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
+                                 nbins, gh, vo, vi, vend, oor_total);
         else
-          pair_loop<false, false>(bj, TJ.y, x, y, z, jlim, inv, base, wl, kb,
-                                  nbins, sh, gh, my_oor);
+          pair_loop<false, false>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
+                                  nbins, gh, vo, vi, vend, oor_total);
       }
     }
-    my_oor = __reduce_add_sync(0xffffffffu, my_oor);
-    if (lane == 0 && my_oor) atomicAdd(&s_oor, my_oor);
     __syncthreads();
     unsigned *dst = partial + (size_t)t * (size_t)words_per_task;
     for (int i = threadIdx.x; i < nw; i += kHistThreads) dst[i] = sh[i];
-    if (threadIdx.x == 0 && s_oor)
-      atomicAdd(oor_total, (unsigned long long)s_oor);
+    if (warp == 0) {  // out-of-range counts: spare words and bin wl
+      const unsigned w = sh[nw + lane];
+      unsigned o = (w & 0xFFFFu) + (w >> 16);
+      if (lane == 0 && (wl & 1u)) o += sh[nw - 1] >> 16;
+      o = __reduce_add_sync(0xffffffffu, o);
+      if (lane == 0 && o) atomicAdd(oor_total, (unsigned long long)o);
+    }
     __syncthreads();
   }
 }
@@ -183,7 +243,7 @@ __global__ void hist_reduce_kernel(const unsigned *__restrict__ partial,
     }
     unsigned long long *g = sg.out + sg.kb + 2 * i;
     g[0] += lo;
-    g[1] += hi;
+    if (2 * i + 1 < sg.wl) g[1] += hi;  // bin wl (odd wl) counts range errors
   }
 }
 
@@ -210,6 +270,58 @@ __global__ void plain_pairs_kernel(const float4 *__restrict__ atoms, long long a
     atomicAdd(&out[k], 1ull);
   else
     atomicAdd(oor, 1ull);
+}
+
+// Self-check of sqrt_rn against the IEEE square root for the floats with
+// bits in [lo, hi] (non-negative: hi <= bits of +inf). res[0] counts
+// mismatches, res[1] keeps the smallest mismatching bits. Inputs below
+// 2^-75 only need a result below 2^-37 (they bin to 0 either way); +inf only
+// a non-finite result.
+__global__ void check_sqrt_kernel(unsigned lo, unsigned hi,
+                                  unsigned long long *res) {
+  const unsigned long long n = (unsigned long long)(hi - lo) + 1ull;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x +
+                              threadIdx.x;
+       i < n; i += stride) {
+    const unsigned u = lo + (unsigned)i;
+    const float s = __uint_as_float(u);
+    const float a = sqrt_rn(s), b = __fsqrt_rn(s);
+    bool good;
+    if (!(s >= 0x1p-75f))
+      good = a < 0x1p-37f;
+    else if (isinf(b))
+      good = !isfinite(a);
+    else
+      good = __float_as_uint(a) == __float_as_uint(b);
+    if (!good) {
+      atomicAdd(&res[0], 1ull);
+      atomicMin(&res[1], (unsigned long long)u);
+    }
+  }
+}
+
+Error check_sqrt(unsigned lo, unsigned hi, int num_sms, cudaStream_t stream,
+                 int64_t out[3]) {
+  if (lo > hi || hi > 0x7F800000u)
+    return fail(DBX_ERR_ARG, "need lo <= hi <= 0x7F800000 (non-negative floats)");
+  unsigned long long *res = nullptr;
+  DBX_CUDA_TRY(cudaMallocAsync((void **)&res, 2 * sizeof(unsigned long long), stream));
+  cudaMemsetAsync(res, 0, sizeof(unsigned long long), stream);
+  cudaMemsetAsync(res + 1, 0xFF, sizeof(unsigned long long), stream);
+  check_sqrt_kernel<<<num_sms * 8, 256, 0, stream>>>(lo, hi, res);
+  cudaError_t e = cudaGetLastError();
+  unsigned long long h[2] = {0, 0};
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, stream);
+  cudaFreeAsync(res, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess)
+    return fail(DBX_ERR_CUDA, std::string("check_sqrt: ") + cudaGetErrorString(e));
+  out[0] = (int64_t)(hi - lo) + 1;
+  out[1] = (int64_t)h[0];
+  out[2] = h[0] ? (int64_t)h[1] : -1;
+  return ok();
 }
 
 // ---------------------------------------------------------------------------
@@ -433,7 +545,8 @@ Error hist_launch(const HistPlan &plan, const HistWorkspace &lists,
   if (ntasks == 0) return ok();
   const int grid = std::min(ntasks, num_sms);
   tm->start(DBX_T_HIST, stream);
-  hist_tiles_kernel<<<grid, kHistThreads, words * 4, stream>>>(
+  hist_tiles_kernel<<<grid, kHistThreads, (words + kSpareWords) * 4,
+                      stream>>>(
       (const int2 *)lists.items.p, (const HistTask *)lists.tasks.p, ntasks,
       (const HistSeg *)lists.segs.p, inv_rstep, (unsigned *)ws->partial.p,
       words, (unsigned long long *)ws->oor.p,

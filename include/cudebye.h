@@ -155,6 +155,17 @@ int64_t dbx_channels(double rmax, double rstep);
 int dbx_reduce_check(const int64_t *counts, int64_t nbins, double rstep,
                      int64_t n_row, int64_t n_col, int diag, int64_t out[4]);
 
+/* Device self-check of the square root inside the histogram kernels (a
+ * branch-free FMA-corrected form, not the library sqrtf): compares it bit
+ * for bit with the IEEE square root for every float whose bits lie in
+ * [lo_bits, hi_bits], 0 <= lo_bits <= hi_bits <= 0x7F800000 (+inf). Inputs
+ * below 2^-75 only need a result below 2^-37 (every bin made from them is
+ * 0), +inf only a non-finite one. out = {inputs checked, mismatches, bits of
+ * the smallest mismatch or -1}. No counterpart in the reference, which
+ * calls sqrtf (cuDebye-v15.cu:101-107). */
+int dbx_check_sqrt(dbx_ctx *ctx, uint32_t lo_bits, uint32_t hi_bits,
+                   int64_t out[3]);
+
 /* ---- hot path 2: Debye sum -------------------------------------------- */
 
 /* 2theta grid and K = 4 pi sin(theta)/lambda (cuDebye-v15.cu:690-698).

@@ -107,6 +107,71 @@ print("OK")
     assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
 
 
+WRAP_EDGE = r"""
+import numpy as np, re, sys
+sys.path.insert(0, %r)
+import cudebye_gb300 as cd
+from oracle import pyoracle as orc
+n0, n1, n2 = 6000, 6000, 3000
+xyz = np.zeros((n0 + n1 + n2, 3), np.float32)
+xyz[n0:n0 + n1, 0] = 6.0
+xyz[n0 + n1:, 0] = 8.0
+counts = [n0, n1, n2]
+with cd.Engine(0) as e:
+    m = e.upload(xyz, counts)
+    # 7 bins (odd): the 36M pairs 0-1 all bin at 6, the last bin, whose low
+    # half carries into the window's spare half (bin 7) on every wrap;
+    # none of that is out of range. 0-2 pairs bin at 8: out of range.
+    try:
+        e.histogram(m, 1.0, 7)
+        raise SystemExit("no range error")
+    except cd.DebyeError as err:
+        assert err.code == -7, err
+        got_bad = int(re.search(r"(\d+) distances", str(err)).group(1))
+    _, bad = orc.model_histograms(xyz, counts, 1.0, 7)
+    assert got_bad == bad == n0 * n2, (got_bad, bad)
+    # 9 bins: everything in range, exact
+    got = e.histogram(m, 1.0, 9)
+    want, bad = orc.model_histograms(xyz, counts, 1.0, 9)
+    assert bad == 0
+    np.testing.assert_array_equal(got, want)
+    # 6 bins: the 36M pairs at 6 are out of range; every lane's clamp lands
+    # on the same spare word, which wraps many times: the count stays exact
+    try:
+        e.histogram(m, 1.0, 6)
+        raise SystemExit("no range error")
+    except cd.DebyeError as err:
+        got_bad = int(re.search(r"(\d+) distances", str(err)).group(1))
+    _, bad = orc.model_histograms(xyz, counts, 1.0, 6)
+    assert got_bad == bad == n0 * n1 + n0 * n2, (got_bad, bad)
+print("OK")
+"""
+
+
+def test_wraps_at_the_window_edge(orc):
+    """Counter wraps in the last bin of an odd-sized window (its carry goes
+    to the spare half past the window and must not count as a range error),
+    and exact range-error counts when tens of millions of pairs fall beyond
+    rmax into the same spare counter. Few tasks, so each wraps often."""
+    code = WRAP_EDGE % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, DBX_HIST_TASKS="3")
+    r = subprocess.run(["python", "-c", code], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
+def test_kernel_sqrt_is_ieee_for_every_float(engine):
+    """The histogram kernels' branch-free square root equals the IEEE
+    sqrtf bit for bit on every non-negative float (2^31 - 2^23 + 1
+    inputs)."""
+    checked, bad, first = engine.check_sqrt()
+    assert checked == 0x7F800001
+    assert bad == 0, "first mismatch at bits 0x%08x" % first
+    with pytest.raises(cd.DebyeError) as e:
+        engine.check_sqrt(0x80000000, 0x80000001)  # negative floats: refused
+    assert e.value.code == -1
+
+
 def test_out_of_range_is_an_error(engine):
     """A distance beyond rmax: the reference writes out of bounds
     (README.md, "Third Line"); the engine returns DBX_ERR_RANGE."""
