@@ -33,6 +33,29 @@ sys.path.insert(0, ROOT)
 
 METRIC = "G binned pairs/s"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# DRAM bytes per launch of the top kernels, from ncu captures (see the
+# summaries beside it); keyed by kernel, then workload.
+TRAFFIC_PATH = os.path.join(ROOT, "profiles", "traffic.json")
+
+
+def measured_traffic(kernel, workload):
+    try:
+        with open(TRAFFIC_PATH) as f:
+            t = json.load(f)
+        return t[kernel][workload]["dram_bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def launches_per_pattern(mode, npairs):
+    """Kernels one dbx_pattern call launches on a resident model whose q grid
+    is unchanged: the histogram (zero, tiles, reduce), the prefactor, then
+    for the tensor-core sum the self term, weights, contraction and reduce,
+    for the direct sums one launch per 16 pair types."""
+    n = 3 + 1
+    if mode == "tc":
+        return n + 4
+    return n + (npairs + 15) // 16
 
 
 def peaks():
@@ -417,34 +440,38 @@ def run_engine(args):
     pk, pk_kind = peaks()
     clocks = clk.summary()
     ph = {k: float(np.mean(v)) for k, v in phase.items()}
+    npair_types = len(m.counts) * (len(m.counts) + 1) // 2
     total_pairs = m.pairs * ws
     value = total_pairs / t_step / 1e9
-    # roofline of the dominant kernel
-    dom = max(ph, key=ph.get)
+    # roofline of the dominant kernel (the histogram), and of the
+    # tensor-core contraction beside it
     sm_mhz = clocks["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)
-    if dom in ("hist", "hist_reduce"):
-        # FP32-pipe issue bound of the reference's exact bin formula:
-        # 16 FP32-pipe operations per pair (3 sub, 3 mul, 2 add, IEEE sqrt
-        # as approximation + 3 correction ops, 1 mul, exact roundf 4 ops),
-        # 152 SMs x 128 lanes per clock.
-        ops = 16
-        peak = 152 * 128 * sm_mhz * 1e6 / ops / 1e9
-        ach = m.pairs / (ph["hist"] / 1e3) / 1e9
-        roof = {"kernel": "hist_tiles_kernel", "bound": "alu",
-                "achieved": ach, "peak": peak, "unit": "Gpair/s",
-                "frac": ach / peak, "traffic": None,
-                "peak_basis": "FP32 pipe, %d ops/pair at %.0f MHz (median "
-                              "sampled)" % (ops, sm_mhz)}
-    else:
-        q, nb = len(K), m.nbins
-        npair = len(m.counts) * (len(m.counts) + 1) // 2
-        flops = 2.0 * q * nb * npair
-        ach = flops / (ph["debye"] / 1e3) / 1e12
-        peak = pk["bf16_tflops"]
-        roof = {"kernel": "debye", "bound": "tensor", "achieved": ach,
-                "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "traffic": None,
-                "peak_basis": "bf16 dense, %s" % pk_kind}
+    # FP32-pipe bound of the reference's exact bin formula: 16 FP32
+    # operations per pair (3 sub, 3 mul, 2 add, square root as estimate + 4
+    # correction ops, 1 mul, 2 for roundf), 152 SMs x 128 FP32 lanes per
+    # clock. Packed FP32x2 instructions do two of these per lane and issue
+    # slot, so a kernel can exceed this bound.
+    ops = 16
+    peak = 152 * 128 * sm_mhz * 1e6 / ops / 1e9
+    ach = m.pairs / (ph["hist"] / 1e3) / 1e9
+    roof = {"kernel": "hist_tiles_kernel", "bound": "alu",
+            "achieved": ach, "peak": peak, "unit": "Gpair/s",
+            "frac": ach / peak,
+            "traffic": measured_traffic("hist_tiles_kernel", m.label),
+            "traffic_unit": "DRAM bytes per launch (ncu)",
+            "algorithmic_bytes": 16 * m.natoms + 8 * m.nbins * npair_types,
+            "peak_basis": "FP32 pipe, %d ops/pair at %.0f MHz (median "
+                          "sampled SM clock)" % (ops, sm_mhz)}
+    flops = 2.0 * len(K) * m.nbins * npair_types
+    tc_ach = flops / (ph["debye"] / 1e3) / 1e12
+    roof_tc = {"kernel": "debye (weights + gemm + reduce)", "bound": "tensor",
+               "achieved": tc_ach, "peak": pk["bf16_tflops"],
+               "unit": "TFLOP/s", "frac": tc_ach / pk["bf16_tflops"],
+               "traffic": measured_traffic("gemm_kernel", m.label),
+               "flops_basis": "2 x q x bins x pair types (one FP64-exact "
+                              "sinc product per count); the split form "
+                              "issues 10 bf16 MMAs per product",
+               "peak_basis": "bf16 dense, %s" % pk_kind}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
@@ -463,8 +490,9 @@ def run_engine(args):
                 "h2d_bytes_per_step": (h2d1 - h2d0) // args.steps,
                 "d2h_bytes_per_step": (d2h1 - d2h0) // args.steps,
                 "ms_per_step": t_e2e * 1e3},
-        "gpu_launches": args.steps * (3 + (len(m.counts) * (len(m.counts) + 1) // 2 + 15) // 16),
+        "gpu_launches": args.steps * launches_per_pattern(mode, npair_types),
         "roofline": roof,
+        "roofline_debye": roof_tc,
         "clocks": clocks,
     }
     if not args.no_cpu:
