@@ -280,7 +280,7 @@ Error batch_device_pass(dbx_ctx *c, dbx::Timers *tm) {
 // keep the fastest (tasks per SM).
 Error autotune_tasks(dbx_ctx *c) {
   BatchState &b = c->batch;
-  const int cand[3] = {2, 4, 8};
+  const int cand[3] = {4, 8, 16};
   float best = 1e30f;
   int best_t = c->hist_tasks;
   cudaEvent_t e0, e1;

@@ -125,8 +125,14 @@ struct HistSeg {  // one (model, pair, bin window) accumulated in smem
   int wl;                   // window length in bins
   int task_begin, task_end;
   unsigned nbins;           // bins of this histogram
-  int pad;
+  // Item source: kSegList reads {I, J | diag << 31} from the plan's item
+  // list; kSegRect enumerates tiles ti0 + [0, tni) x tj0 + [0, tnj) and
+  // kSegTri the pairs I <= J of ti0 + [0, tni) (a species with itself),
+  // item index = task-local position.
+  int shape;
+  int ti0, tni, tj0, tnj;
 };
+constexpr int kSegList = 0, kSegRect = 1, kSegTri = 2;
 struct HistTask {  // one CTA-sized slice of a segment's tile pairs
   int seg;
   int item_begin, item_end;
@@ -141,7 +147,9 @@ struct HistPlan {
   std::vector<int2> items;     // {tile I, tile J | (diag << 31)}
   std::vector<int> item_pairs; // pairs of each item (host only)
   std::vector<HistSeg> segs;
-  std::vector<int2> seg_items; // item range of each segment (host only)
+  std::vector<int2> seg_items; // item range of each segment (host only;
+                               // [0, count) for enumerated segments)
+  std::vector<int64_t> seg_pairs; // binned pairs of each segment (host only)
   std::vector<HistTask> tasks;
   std::vector<HistRow> rows;
   int window = 0;              // largest window in bins

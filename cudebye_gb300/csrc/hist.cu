@@ -136,6 +136,25 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
   }
 }
 
+// Item it_i of a segment: {tile I (rows), tile J (columns) | diag << 31}.
+__device__ __forceinline__ int2 seg_item(const HistSeg &sg,
+                                         const int2 *__restrict__ items,
+                                         int it_i) {
+  if (sg.shape == kSegList) return __ldg(&items[it_i]);
+  if (sg.shape == kSegRect)
+    return make_int2(sg.ti0 + it_i / sg.tnj, sg.tj0 + it_i % sg.tnj);
+  // triangle row-major by J: item t = J (J + 1) / 2 + I, I <= J. The FP32
+  // estimate of J is off by at most one for t < 2^31 and is corrected in
+  // integers (an FP64 square root here would queue every warp of a CTA on
+  // the slow FP64 pipe at each task start).
+  int j = (int)((sqrtf(8.0f * (float)it_i + 1.0f) - 1.0f) * 0.5f);
+  while ((long long)j * (j + 1) / 2 > it_i) --j;
+  while ((long long)(j + 1) * (j + 2) / 2 <= it_i) ++j;
+  const int i = it_i - j * (j + 1) / 2;
+  return make_int2(sg.ti0 + i,
+                   (sg.ti0 + j) | (i == j ? int(0x80000000u) : 0));
+}
+
 // One warp = one tile pair (128 x 128 atoms). CTAs pull equal-sized tasks
 // from a global counter; task t's packed window goes to partial slot t.
 __global__ void __launch_bounds__(kHistThreads, 1)
@@ -175,7 +194,7 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     const bool full_window = kb == 0 && wl >= nbins;
     for (int it_i = tk.item_begin + warp; it_i < tk.item_end;
          it_i += kHistThreads / 32) {
-      const int2 it = __ldg(&items[it_i]);
+      const int2 it = seg_item(sg, items, it_i);
       const bool diag = it.y < 0;
       const int2 TI = __ldg(&tiles[it.x]);
       const int2 TJ = __ldg(&tiles[it.y & 0x7fffffff]);
@@ -352,6 +371,7 @@ void hist_plan_clear(HistPlan *plan) {
   plan->item_pairs.clear();
   plan->segs.clear();
   plan->seg_items.clear();
+  plan->seg_pairs.clear();
   plan->tasks.clear();
   plan->rows.clear();
   plan->pairs = 0;
@@ -375,6 +395,38 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
     const int a = pairs[pi].x, b = pairs[pi].y;
     unsigned long long *row = out + (int64_t)pi * pitch;
     plan->rows.push_back(HistRow{row, pitch});
+    const int64_t na = m.sp_count[a], nb = m.sp_count[b];
+    const int64_t block_pairs = (a == b) ? na * (na + 1) / 2 : na * nb;
+    if (nwin == 1) {
+      // One window holds every bin: the segment's items are all its tile
+      // pairs, enumerated by the kernel (no list, no bounding-box test).
+      const int I0 = m.tile_start[a], nI = m.tile_start[a + 1] - I0;
+      const int J0 = m.tile_start[b], nJ = m.tile_start[b + 1] - J0;
+      const int64_t count = (a == b) ? (int64_t)nI * (nI + 1) / 2 : (int64_t)nI * nJ;
+      if (count >= (int64_t(1) << 31))
+        return fail(DBX_ERR_ARG, "too many tile pairs in one species pair");
+      if (count > 0) {
+        HistSeg s;
+        s.atoms = m.d_atoms;
+        s.tiles = m.d_tiles;
+        s.out = row;
+        s.kb = 0;
+        s.wl = (int)nbins;
+        s.task_begin = s.task_end = 0;
+        s.nbins = (unsigned)nbins;
+        s.shape = (a == b) ? kSegTri : kSegRect;
+        s.ti0 = I0;
+        s.tni = nI;
+        s.tj0 = J0;
+        s.tnj = nJ;
+        plan->segs.push_back(s);
+        plan->seg_items.push_back(make_int2(0, (int)count));
+        plan->seg_pairs.push_back(block_pairs);
+      }
+      plan->pairs += block_pairs;
+      plan->nrows += 1;
+      continue;
+    }
     for (auto &v : per_win) v.clear();
     for (int I = m.tile_start[a]; I < m.tile_start[a + 1]; ++I) {
       const int J0 = (a == b) ? I : m.tile_start[b];
@@ -404,18 +456,21 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       s.wl = (int)std::min<int64_t>(W, nbins - w * W);
       s.task_begin = s.task_end = 0;
       s.nbins = (unsigned)nbins;
-      s.pad = 0;
+      s.shape = kSegList;
+      s.ti0 = s.tni = s.tj0 = s.tnj = 0;
       const int first = (int)plan->items.size();
+      int64_t sp = 0;
       for (const int2 &it : per_win[w]) {
         const int2 TI = m.tiles[it.x], TJ = m.tiles[it.y & 0x7fffffff];
         plan->items.push_back(it);
         plan->item_pairs.push_back((int)item_pairs(TI.y, TJ.y, it.y < 0));
+        sp += plan->item_pairs.back();
       }
       plan->segs.push_back(s);
       plan->seg_items.push_back(make_int2(first, (int)plan->items.size()));
+      plan->seg_pairs.push_back(sp);
     }
-    const int64_t na = m.sp_count[a], nb = m.sp_count[b];
-    plan->pairs += (a == b) ? na * (na + 1) / 2 : na * nb;
+    plan->pairs += block_pairs;
     plan->nrows += 1;
   }
   return ok();
@@ -423,15 +478,12 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
 
 void hist_plan_tasks(HistPlan *plan, int target_tasks) {
   // Split every segment into n_s tasks of about equal pair counts, n_s
-  // from the segment's share of about target_tasks tasks in all.
+  // from the segment's share of about target_tasks tasks in all. Listed
+  // items are split by their pair counts; enumerated segments (nearly all
+  // items full 128 x 128 tile pairs) by item count.
   plan->tasks.clear();
-  std::vector<int64_t> seg_pairs(plan->segs.size(), 0);
   int64_t total = 0;
-  for (size_t s = 0; s < plan->segs.size(); ++s) {
-    for (int i = plan->seg_items[s].x; i < plan->seg_items[s].y; ++i)
-      seg_pairs[s] += plan->item_pairs[i];
-    total += seg_pairs[s];
-  }
+  for (int64_t p : plan->seg_pairs) total += p;
   const double target =
       std::max(1.0, (double)total / std::max(1, target_tasks));
   for (size_t s = 0; s < plan->segs.size(); ++s) {
@@ -439,16 +491,25 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
     sg.task_begin = (int)plan->tasks.size();
     const int i0 = plan->seg_items[s].x, i1 = plan->seg_items[s].y;
     const int64_t n_s = std::max<int64_t>(
-        1, std::min<int64_t>(i1 - i0, (int64_t)std::llround(seg_pairs[s] / target)));
-    int64_t acc = 0, k = 1;
-    int begin = i0;
-    for (int i = i0; i < i1; ++i) {
-      acc += plan->item_pairs[i];
-      // close task k when the running sum reaches k/n_s of the segment
-      if (i + 1 == i1 || (k < n_s && acc * n_s >= k * seg_pairs[s])) {
-        plan->tasks.push_back(HistTask{(int)s, begin, i + 1, 0});
-        begin = i + 1;
-        ++k;
+        1, std::min<int64_t>(i1 - i0,
+                             (int64_t)std::llround(plan->seg_pairs[s] / target)));
+    if (sg.shape != kSegList) {
+      for (int64_t k = 0; k < n_s; ++k) {
+        const int b = (int)(i0 + (i1 - i0) * k / n_s);
+        const int e = (int)(i0 + (i1 - i0) * (k + 1) / n_s);
+        if (e > b) plan->tasks.push_back(HistTask{(int)s, b, e, 0});
+      }
+    } else {
+      int64_t acc = 0, k = 1;
+      int begin = i0;
+      for (int i = i0; i < i1; ++i) {
+        acc += plan->item_pairs[i];
+        // close task k when the running sum reaches k/n_s of the segment
+        if (i + 1 == i1 || (k < n_s && acc * n_s >= k * plan->seg_pairs[s])) {
+          plan->tasks.push_back(HistTask{(int)s, begin, i + 1, 0});
+          begin = i + 1;
+          ++k;
+        }
       }
     }
     sg.task_end = (int)plan->tasks.size();
@@ -493,9 +554,10 @@ Error hist_upload(const HistPlan &plan, HistWorkspace *ws, cudaStream_t stream,
                                  plan.rows.size() * sizeof(HistRow),
                                  cudaMemcpyHostToDevice, stream));
   if (ntasks == 0) return ok();
-  DBX_CUDA_TRY(cudaMemcpyAsync(ws->items.p, plan.items.data(),
-                               plan.items.size() * sizeof(int2),
-                               cudaMemcpyHostToDevice, stream));
+  if (!plan.items.empty())
+    DBX_CUDA_TRY(cudaMemcpyAsync(ws->items.p, plan.items.data(),
+                                 plan.items.size() * sizeof(int2),
+                                 cudaMemcpyHostToDevice, stream));
   DBX_CUDA_TRY(cudaMemcpyAsync(ws->segs.p, plan.segs.data(),
                                nsegs * sizeof(HistSeg), cudaMemcpyHostToDevice,
                                stream));

@@ -47,7 +47,8 @@ Error model_prepare(const float *x, const float *y, const float *z,
   const double scale = ext > 0 ? 1023.0 / ext : 0.0;
   std::vector<float4> &atoms = *atoms_out;
   atoms.assign(std::max<int64_t>(natoms, 1), make_float4(0, 0, 0, 0));
-  std::vector<uint64_t> key;
+  std::vector<uint32_t> code, code2;
+  std::vector<int32_t> idx, idx2;
   int64_t start = 0;
   m->tile_start.assign(1, 0);
   m->tiles.clear();
@@ -56,8 +57,12 @@ Error model_prepare(const float *x, const float *y, const float *z,
   m->sp_count.clear();
   for (int s = 0; s < nspecies; ++s) {
     const int64_t n = counts[s];
-    // (code << 32 | index): one sort gives a stable Morton order
-    key.resize(n);
+    // 30-bit Morton codes, then a stable LSD radix sort (three 10-bit
+    // passes): atoms with equal codes keep their input order.
+    code.resize(n);
+    code2.resize(n);
+    idx.resize(n);
+    idx2.resize(n);
     for (int64_t i = 0; i < n; ++i) {
       uint32_t q[3];
       for (int d = 0; d < 3; ++d) {
@@ -65,12 +70,23 @@ Error model_prepare(const float *x, const float *y, const float *z,
         t = std::isfinite(t) ? std::min(std::max(t, 0.0), 1023.0) : 0.0;
         q[d] = (uint32_t)t;
       }
-      const uint64_t code = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
-      key[i] = (code << 32) | (uint64_t)i;
+      code[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+      idx[i] = (int32_t)i;
     }
-    std::sort(key.begin(), key.end());
+    for (int shift = 0; shift < 30; shift += 10) {
+      int64_t hist[1025] = {0};
+      for (int64_t i = 0; i < n; ++i) ++hist[((code[i] >> shift) & 1023u) + 1];
+      for (int b = 0; b < 1024; ++b) hist[b + 1] += hist[b];
+      for (int64_t i = 0; i < n; ++i) {
+        const int64_t o = hist[(code[i] >> shift) & 1023u]++;
+        code2[o] = code[i];
+        idx2[o] = idx[i];
+      }
+      code.swap(code2);
+      idx.swap(idx2);
+    }
     for (int64_t i = 0; i < n; ++i) {
-      const int64_t src = start + (int64_t)(key[i] & 0xffffffffu);
+      const int64_t src = start + idx[i];
       atoms[start + i] = make_float4(x[src], y[src], z[src], 0.f);
     }
     m->sp_start.push_back(start);
