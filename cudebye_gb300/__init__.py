@@ -52,7 +52,8 @@ EXPORTS = (
     "dbx_run_deb", "dbx_pair_histogram_noalloc", "dbx_patterns",
     "dbx_set_graphs", "dbx_server_create", "dbx_server_submit",
     "dbx_server_wait", "dbx_server_stats", "dbx_server_destroy",
-    "dbx_check_sqrt",
+    "dbx_check_sqrt", "dbx_xyz2deb", "dbx_xyz2deb_defaults", "dbx_deb_pack",
+    "dbx_run_dir",
 )
 TIMERS = ("hist", "hist_reduce", "prefactor", "debye", "pass")
 
@@ -97,6 +98,15 @@ class Request(ctypes.Structure):
 
 
 _lib = None
+
+
+class XyzDebParams(ctypes.Structure):
+    """dbx_xyz2deb_params: the header values of a converted .deb."""
+    _fields_ = [("device", ctypes.c_int), ("block", ctypes.c_int),
+                ("grid", ctypes.c_int), ("lam", ctypes.c_double),
+                ("tt_min", ctypes.c_double), ("tt_max", ctypes.c_double),
+                ("tt_step", ctypes.c_double), ("rstep", ctypes.c_double),
+                ("intensity", ctypes.c_int), ("distances", ctypes.c_int)]
 
 
 def load_library(path=None):
@@ -151,6 +161,8 @@ def load_library(path=None):
         "dbx_get_traffic": (ctypes.c_int, [c_p, i64p]),
         "dbx_run_deb": (ctypes.c_int, [c_p, ctypes.c_char_p, ctypes.c_char_p,
                                        ctypes.c_int]),
+        "dbx_run_dir": (ctypes.c_int, [c_p, ctypes.c_char_p, ctypes.c_char_p,
+                                       ctypes.c_int]),
         "dbx_patterns": (ctypes.c_int, [c_p, i64p, ctypes.c_int,
                                         ctypes.c_double, i64p,
                                         ctypes.POINTER(Species), dp,
@@ -169,6 +181,13 @@ def load_library(path=None):
         "dbx_pair_histogram_noalloc": (ctypes.c_int, [
             c_p, c_p, c_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
             ctypes.c_int64, ctypes.c_double, ctypes.c_int64, c_p, c_p]),
+        "dbx_xyz2deb_defaults": (None, [ctypes.POINTER(XyzDebParams)]),
+        "dbx_deb_pack": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p,
+                                        ctypes.c_char_p, ctypes.c_size_t]),
+        "dbx_xyz2deb": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p,
+                                       ctypes.POINTER(XyzDebParams),
+                                       ctypes.c_char_p, ctypes.c_char_p,
+                                       ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -227,6 +246,66 @@ class DebFile:
         self.hist = 0
         self.names, self.counts, self.species = [], [], []
         self.xyz = np.zeros((0, 3), np.float32)
+
+
+def xyz2deb(xyz_path, table_path, deb_path=None, **params):
+    """The reference's Matlab converter (Matlab/xyz2deb.m): write a .deb from
+    an "element x y z [occ [Beq]]" file and a Waasmaier-Kirfel table in the
+    RIETAN layout. Keyword arguments override the script's defaults (device,
+    block, grid, lam, tt_min, tt_max, tt_step, rstep, intensity,
+    distances). Returns the .deb path. Needs no GPU."""
+    lib = load_library()
+    p = XyzDebParams()
+    lib.dbx_xyz2deb_defaults(ctypes.byref(p))
+    for k, v in params.items():
+        if not hasattr(p, k):
+            raise TypeError("unknown xyz2deb parameter %r" % k)
+        setattr(p, k, v)
+    msg = ctypes.create_string_buffer(512)
+    rc = lib.dbx_xyz2deb(xyz_path.encode(), table_path.encode(),
+                         ctypes.byref(p),
+                         deb_path.encode() if deb_path else None, msg, 512)
+    if rc != DBX_OK:
+        raise DebyeError(rc, msg.value.decode(errors="replace"))
+    return deb_path or (xyz_path[:-3] + "deb")
+
+
+def deb_pack(deb_path, out_path):
+    """Write the binary form of a .deb (dbx_deb_pack). Needs no GPU."""
+    lib = load_library()
+    msg = ctypes.create_string_buffer(512)
+    rc = lib.dbx_deb_pack(deb_path.encode(), out_path.encode(), msg, 512)
+    if rc != DBX_OK:
+        raise DebyeError(rc, msg.value.decode(errors="replace"))
+    return out_path
+
+
+def read_debb(path):
+    """Parse the binary form written by deb_pack into a DebFile."""
+    import struct
+    with open(path, "rb") as f:
+        b = f.read()
+    if b[:8] != b"DBXDEB1\0":
+        raise DebyeError(-5, "not a binary .deb")
+    d = DebFile()
+    d.device, d.block, d.grid, d.hist = struct.unpack_from("<4i", b, 8)
+    (d.lam, d.tt_min, d.tt_max, d.tt_step, d.rmax,
+     d.rstep) = struct.unpack_from("<6d", b, 24)
+    nsp, _ = struct.unpack_from("<2i", b, 72)
+    pos = 80
+    d.counts, d.names, d.species = [], [], []
+    for _ in range(nsp):
+        n, = struct.unpack_from("<q", b, pos)
+        name = b[pos + 8:pos + 40].split(b"\0")[0].decode()
+        v = struct.unpack_from("<13d", b, pos + 40)
+        pos += 144
+        d.counts.append(n)
+        d.names.append(name)
+        d.species.append(Species.make(v[0], v[1], v[2:7], v[7:12], v[12]))
+    N = sum(d.counts)
+    xyz = np.frombuffer(b, np.float32, 3 * N, pos).reshape(3, N)
+    d.xyz = np.ascontiguousarray(xyz.T)
+    return d
 
 
 def read_deb(path):
@@ -440,6 +519,13 @@ class Engine:
         self._check(self.lib.dbx_run_deb(
             self.ctx, path.encode(),
             out_prefix.encode() if out_prefix else None, int(verbose)))
+
+    def run_dir(self, folder, table=None, verbose=False):
+        """The reference's multisim: convert .xyz without .deb (with a
+        scattering-factor table), compute every .deb without .debI."""
+        self._check(self.lib.dbx_run_dir(
+            self.ctx, folder.encode(), table.encode() if table else None,
+            int(verbose)))
 
 
 class Server:

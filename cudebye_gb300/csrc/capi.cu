@@ -1,11 +1,14 @@
 // capi.cu — context, resident models and the C ABI (include/cudebye.h).
 #include <cuda_runtime.h>
+#include <dirent.h>
+#include <sys/stat.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <future>
 #include <map>
 #include <memory>
 #include <numeric>
@@ -856,17 +859,21 @@ int dbx_run_deb(dbx_ctx *c, const char *deb_path, const char *out_prefix,
     if (verbose) printf("\nERROR: %s\n", e.msg.c_str());
     return set_err(c, e);
   }
+  // All pair histograms to the host at once; the .debx files are then
+  // written by one thread each while the Debye sum runs on the device.
+  const int np = dbx::npairs_of(P);
+  std::vector<int64_t> h;
+  std::vector<std::future<int>> writers;
   if (d.hist > 0 || verbose) {
-    std::vector<int64_t> h(nbins);
+    h.resize((size_t)np * nbins);
+    e = copy_rows(c, m->d_hist, m->hist_pitch, nbins, np, h.data());
+    if (e.code) return set_err(c, e);
     for (int row = 0; row < P; ++row)
       for (int col = row; col < P; ++col) {
-        const int p = dbx::pair_index(P, row, col);
-        e = copy_rows(c, m->d_hist + (size_t)p * m->hist_pitch, m->hist_pitch,
-                      nbins, 1, h.data());
-        if (e.code) return set_err(c, e);
+        const int64_t *hp = h.data() + (size_t)dbx::pair_index(P, row, col) * nbins;
         if (verbose) {
           int64_t chk[4];
-          dbx_reduce_check(h.data(), nbins, d.rstep, counts[row], counts[col],
+          dbx_reduce_check(hp, nbins, d.rstep, counts[row], counts[col],
                            row == col, chk);
           printf("\n>>>> Subgroup %d and %d\n", row, col);
           if (chk[0] != chk[1])
@@ -886,26 +893,231 @@ int dbx_run_deb(dbx_ctx *c, const char *deb_path, const char *out_prefix,
         if (d.hist > 0) {
           const std::string path =
               prefix + "x" + std::to_string(row) + "x" + std::to_string(col);
-          if (dbx::write_debx(path, h.data(), nbins, d.rstep))
-            return set_err(c, dbx::fail(DBX_ERR_IO, "cannot write " + path));
+          const double rstep = d.rstep;
+          writers.push_back(std::async(std::launch::async, [=]() {
+            return dbx::write_debx(path, hp, nbins, rstep);
+          }));
         }
       }
   }
+  Error out = dbx::ok();
   if (d.hist != 1) {
     const int nq = dbx_k_grid(d.lambda, d.tt_min, d.tt_max, d.tt_step, nullptr,
                               nullptr);
-    if (nq < 1) return set_err(c, dbx::fail(DBX_ERR_PARSE, "empty 2theta grid"));
-    std::vector<double> tt(nq), K(nq), I(nq);
-    dbx_k_grid(d.lambda, d.tt_min, d.tt_max, d.tt_step, tt.data(), K.data());
-    e = intensity(c, m, d.rstep, nbins, sp.data(), K.data(), nq, DBX_DEBYE_TC,
-                  I.data());
-    if (e.code) return set_err(c, e);
-    const std::string path = prefix + "I";
-    if (dbx::write_debI(path, tt.data(), I.data(), nq))
-      return set_err(c, dbx::fail(DBX_ERR_IO, "cannot write " + path));
-    if (verbose) printf("\nWrote %s (%d points)\n", path.c_str(), nq);
+    if (nq < 1) {
+      out = dbx::fail(DBX_ERR_PARSE, "empty 2theta grid");
+    } else {
+      std::vector<double> tt(nq), K(nq), I(nq);
+      dbx_k_grid(d.lambda, d.tt_min, d.tt_max, d.tt_step, tt.data(), K.data());
+      out = intensity(c, m, d.rstep, nbins, sp.data(), K.data(), nq,
+                      DBX_DEBYE_TC, I.data());
+      const std::string path = prefix + "I";
+      if (!out.code && dbx::write_debI(path, tt.data(), I.data(), nq))
+        out = dbx::fail(DBX_ERR_IO, "cannot write " + path);
+      if (!out.code && verbose) printf("\nWrote %s (%d points)\n", path.c_str(), nq);
+    }
   }
+  for (auto &w : writers)
+    if (w.get() != DBX_OK && !out.code)
+      out = dbx::fail(DBX_ERR_IO, "cannot write a .debx file next to " + prefix);
+  return set_err(c, out);
+}
+
+// ---- directory driver ------------------------------------------------------
+// The reference's Matlab batch driver (Matlab/multisim.m:9-65) without its
+// plots: every .xyz of `dir` without a .deb is converted first (when a
+// scattering-factor table is given), then every .deb without a .debI is
+// computed. Models that share rstep and the 2theta grid are batched
+// (dbx_patterns: one histogram launch and one contraction per chunk of up to
+// kDirChunk models); the outputs of a chunk are written on a host thread
+// while the next chunk runs. A chunk that fails is redone file by file, so
+// one bad file does not stop the others; the first error is returned.
+
+namespace {
+constexpr int kDirChunk = 64;
+
+bool ends_with(const std::string &s, const char *t) {
+  const size_t n = strlen(t);
+  return s.size() >= n && s.compare(s.size() - n, n, t) == 0;
+}
+
+struct DirItem {
+  std::string name, path;
+  dbx::DebFile d;
+};
+
+// Writes the outputs of one model of a chunk: .debx (hist 1/2) and .debI
+// (hist 0/2), from host copies.
+int write_item(const DirItem &it, const std::vector<int64_t> &h, int64_t nbins,
+               const std::vector<double> &tt, const double *I) {
+  const int P = (int)it.d.species.size();
+  if (it.d.hist > 0)
+    for (int row = 0; row < P; ++row)
+      for (int col = row; col < P; ++col) {
+        const std::string path =
+            it.path + "x" + std::to_string(row) + "x" + std::to_string(col);
+        const int64_t *hp = h.data() + (size_t)dbx::pair_index(P, row, col) * nbins;
+        if (dbx::write_debx(path, hp, nbins, it.d.rstep)) return DBX_ERR_IO;
+      }
+  if (it.d.hist != 1 && dbx::write_debI(it.path + "I", tt.data(), I, (int)tt.size()))
+    return DBX_ERR_IO;
   return DBX_OK;
+}
+}  // namespace
+
+extern "C" int dbx_run_dir(dbx_ctx *c, const char *dir, const char *table_path,
+                           int verbose) {
+  if (!c || !dir) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  auto list = [&](std::vector<std::string> *names) {
+    names->clear();
+    DIR *dp = opendir(dir);
+    if (!dp) return false;
+    while (dirent *de = readdir(dp)) {
+      const std::string n = de->d_name;
+      struct stat st;
+      if (stat((std::string(dir) + "/" + n).c_str(), &st) == 0 && S_ISREG(st.st_mode))
+        names->push_back(n);
+    }
+    closedir(dp);
+    std::sort(names->begin(), names->end());
+    return true;
+  };
+  std::vector<std::string> files;
+  if (!list(&files))
+    return set_err(c, dbx::fail(DBX_ERR_FILE, std::string("cannot open ") + dir));
+  int first = DBX_OK;
+  std::string first_msg;
+  auto note = [&](int rc, const std::string &m) {
+    if (rc && !first) {
+      first = rc;
+      first_msg = m;
+    }
+    if (rc && verbose) printf("ERROR: %s\n", m.c_str());
+  };
+  std::vector<std::string> xyz;
+  for (const std::string &f : files)
+    if (ends_with(f, ".xyz") &&
+        !std::binary_search(files.begin(), files.end(), f.substr(0, f.size() - 3) + "deb"))
+      xyz.push_back(f);
+  for (size_t i = 0; i < xyz.size(); ++i) {
+    const std::string path = std::string(dir) + "/" + xyz[i];
+    if (!table_path) {
+      if (verbose) printf("Skip %s: no scattering-factor table given\n", xyz[i].c_str());
+      continue;
+    }
+    if (verbose)
+      printf("Convert File %zu of %zu -- %s\n", i + 1, xyz.size(), xyz[i].c_str());
+    char m[512] = {0};
+    const int rc = dbx_xyz2deb(path.c_str(), table_path, nullptr, nullptr, m, sizeof m);
+    note(rc, m);
+  }
+  if (!list(&files))
+    return set_err(c, dbx::fail(DBX_ERR_FILE, std::string("cannot open ") + dir));
+  std::vector<DirItem> items;
+  for (const std::string &f : files)
+    if (ends_with(f, ".deb") && !std::binary_search(files.begin(), files.end(), f + "I")) {
+      DirItem it;
+      it.name = f;
+      it.path = std::string(dir) + "/" + f;
+      std::string m;
+      const int rc = dbx::deb_read(it.path, &it.d, &m);
+      if (rc) {
+        note(rc, f + ": " + m);
+        continue;
+      }
+      items.push_back(std::move(it));
+    }
+  // groups: same rstep and 2theta grid, in file order
+  std::vector<std::vector<int>> groups;
+  for (int i = 0; i < (int)items.size(); ++i) {
+    const dbx::DebFile &d = items[i].d;
+    bool placed = false;
+    for (auto &g : groups) {
+      const dbx::DebFile &e = items[g[0]].d;
+      if (e.rstep == d.rstep && e.lambda == d.lambda && e.tt_min == d.tt_min &&
+          e.tt_max == d.tt_max && e.tt_step == d.tt_step &&
+          (int)g.size() < kDirChunk) {
+        g.push_back(i);
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) groups.push_back({i});
+  }
+  int done = 0;
+  std::future<int> pending;
+  for (const std::vector<int> &g : groups) {
+    const dbx::DebFile &d0 = items[g[0]].d;
+    const int nq = dbx_k_grid(d0.lambda, d0.tt_min, d0.tt_max, d0.tt_step, nullptr,
+                              nullptr);
+    std::vector<double> tt(std::max(nq, 1)), K(std::max(nq, 1));
+    if (nq >= 1) dbx_k_grid(d0.lambda, d0.tt_min, d0.tt_max, d0.tt_step, tt.data(), K.data());
+    std::vector<int64_t> ids, nb;
+    std::vector<dbx_species> sp;
+    int rc = nq >= 1 ? DBX_OK : DBX_ERR_PARSE;
+    for (int i : g) {
+      if (rc) break;
+      const dbx::DebFile &d = items[i].d;
+      std::vector<int64_t> counts;
+      for (const dbx::DebSpecies &s : d.species) {
+        counts.push_back(s.n);
+        sp.push_back(s.p);
+      }
+      int64_t id = 0;
+      rc = dbx_model_upload(c, d.x.data(), d.y.data(), d.z.data(), counts.data(),
+                            (int)counts.size(), &id);
+      if (!rc) {
+        ids.push_back(id);
+        nb.push_back(dbx_channels(d.rmax, d.rstep));
+      }
+    }
+    std::vector<double> I;
+    if (!rc) {
+      I.resize((size_t)nq * g.size());
+      rc = dbx_patterns(c, ids.data(), (int)ids.size(), d0.rstep, nb.data(), sp.data(),
+                        K.data(), nq, DBX_DEBYE_TC, I.data());
+    }
+    // histograms of the chunk to the host (the writers need them)
+    std::vector<std::vector<int64_t>> hs(g.size());
+    for (size_t k = 0; !rc && k < g.size(); ++k) {
+      dbx::Model *m = find_model(c, ids[k]);
+      const int np = dbx::npairs_of(m->nspecies);
+      hs[k].resize((size_t)np * nb[k]);
+      Error e = copy_rows(c, m->d_hist, m->hist_pitch, nb[k], np, hs[k].data());
+      rc = e.code;
+    }
+    for (int64_t id : ids) dbx_model_free(c, id);
+    if (pending.valid()) note(pending.get(), "cannot write an output file");
+    if (rc) {
+      // isolate the failing file(s)
+      for (int i : g) {
+        if (verbose)
+          printf("Calculate File %d of %zu -- %s\n", ++done, items.size(),
+                 items[i].name.c_str());
+        const int r1 = dbx_run_deb(c, items[i].path.c_str(), nullptr, 0);
+        note(r1, items[i].name + ": " + dbx_last_error(c));
+      }
+      continue;
+    }
+    if (verbose)
+      for (int i : g)
+        printf("Calculate File %d of %zu -- %s\n", ++done, items.size(),
+               items[i].name.c_str());
+    std::vector<int> gi = g;
+    pending = std::async(std::launch::async,
+                         [&items, gi, hs = std::move(hs), nb, tt, I = std::move(I), nq]() {
+                           for (size_t k = 0; k < gi.size(); ++k) {
+                             const int r = write_item(items[gi[k]], hs[k], nb[k], tt,
+                                                      I.data() + k * (size_t)nq);
+                             if (r) return r;
+                           }
+                           return (int)DBX_OK;
+                         });
+  }
+  if (pending.valid()) note(pending.get(), "cannot write an output file");
+  if (first) c->last_error = first_msg;
+  return first;
 }
 
 }  // extern "C"

@@ -24,9 +24,12 @@ struct DebFile {
   std::vector<float> x, y, z;                    // (:819-827)
 };
 
+// Reads a text .deb or its binary form (detected by the "DBXDEB1" magic).
 // Returns DBX_OK, DBX_ERR_FILE, DBX_ERR_PARSE or DBX_ERR_COUNT; msg is set
 // on error.
 int deb_read(const std::string &path, DebFile *out, std::string *msg);
+// Writes the binary form of d (debio.cpp documents the layout).
+int debb_write(const std::string &path, const DebFile &d);
 
 // Non-zero bins as "%.7g\t%lld\n" of (k*rstep, count) (cuDebye-v15.cu:421-423).
 int write_debx(const std::string &path, const int64_t *counts, int64_t nbins,

@@ -280,6 +280,38 @@ int dbx_server_wait(dbx_server *srv, int64_t ticket, double *out_I, int nq,
 int dbx_server_stats(dbx_server *srv, int64_t out[6]);
 int dbx_server_destroy(dbx_server *srv);
 
+/* ---- .xyz -> .deb conversion (host only) -------------------------------- */
+
+/* Header values of the written .deb (Matlab/xyz2deb.m:13-25 defaults via
+ * dbx_xyz2deb_defaults: device 0, block 16, grid 2048, 1.5418 A, 2theta
+ * 10-140 step 0.02, rstep 0.0001, intensity 1, distances 0). */
+typedef struct dbx_xyz2deb_params {
+  int device, block, grid;
+  double lambda, tt_min, tt_max, tt_step, rstep;
+  int intensity; /* write a .debI (hist 0 or 2) */
+  int distances; /* write .debx files (hist 1 or 2) */
+} dbx_xyz2deb_params;
+void dbx_xyz2deb_defaults(dbx_xyz2deb_params *params);
+
+/* The reference's Matlab converter xyz2deb (Matlab/xyz2deb.m:154-263):
+ * "element x y z [occ [Beq]]" records -> species grouped by (element, occ,
+ * Beq), coordinates centred, rmax = 2 ceil(1.025 max r), coefficients from a
+ * Waasmaier-Kirfel table in the RIETAN layout (e.g. the reference's
+ * Matlab/Tables/atomic_scattering_factors_RIETAN.txt). deb_path NULL = the
+ * .xyz path with its last three characters replaced by "deb". params NULL =
+ * the defaults. msg (may be NULL) receives an error text. Needs no GPU. */
+int dbx_xyz2deb(const char *xyz_path, const char *table_path,
+                const dbx_xyz2deb_params *params, const char *deb_path,
+                char *msg, size_t msg_len);
+
+/* The .deb content in binary form (the reference's wish list item "binary
+ * file support", cuDebye-v15.cu:7): reads deb_path (text or binary) and
+ * writes out_path as "DBXDEB1" + header values + species + float32 x[], y[],
+ * z[] (layout in csrc/debio.cpp). dbx_run_deb and the command line take
+ * either form. Needs no GPU. msg (may be NULL) receives an error text. */
+int dbx_deb_pack(const char *deb_path, const char *out_path, char *msg,
+                 size_t msg_len);
+
 /* ---- whole-file drop-in ----------------------------------------------- */
 
 /* The reference's main() (cuDebye-v15.cu:599-1004) on the GPU: read
@@ -288,6 +320,18 @@ int dbx_server_destroy(dbx_server *srv);
  * out_prefix NULL = deb_path, as the reference does. verbose != 0 prints
  * the reference-style progress log to stdout. */
 int dbx_run_deb(dbx_ctx *ctx, const char *deb_path, const char *out_prefix,
+                int verbose);
+
+/* The reference's Matlab batch driver multisim (Matlab/multisim.m:9-65)
+ * without its plots: in directory `dir`, convert every .xyz that has no .deb
+ * (dbx_xyz2deb with its defaults; skipped when table_path is NULL), then
+ * compute every .deb that has no .debI, writing the same outputs as
+ * dbx_run_deb would. Models sharing rstep and the 2theta grid run batched
+ * (dbx_patterns, up to 64 per chunk); outputs are written on a host thread
+ * while the next chunk runs. Every file is attempted; the first error is
+ * returned. The device index on line 1 of the files is not used (ctx's
+ * device is). */
+int dbx_run_dir(dbx_ctx *ctx, const char *dir, const char *table_path,
                 int verbose);
 
 #ifdef __cplusplus

@@ -63,8 +63,57 @@ def lib():
         L.orc_debye_rowsum.restype = None
         L.orc_debye_rowsum.argtypes = [dp, ctypes.c_int, i64p, i64,
                                        ctypes.c_double, dp, ctypes.c_int]
+        L.orc_deb_read.restype = ctypes.c_int
+        L.orc_deb_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(OrcDeb)]
+        L.orc_deb_free.restype = None
+        L.orc_deb_free.argtypes = [ctypes.POINTER(OrcDeb)]
         _lib = L
     return _lib
+
+
+class OrcSpecies(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("name", ctypes.c_char * 32),
+                ("occ", ctypes.c_double), ("beq", ctypes.c_double),
+                ("a", ctypes.c_double * 5), ("b", ctypes.c_double * 5),
+                ("c", ctypes.c_double)]
+
+
+class OrcDeb(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("block", ctypes.c_int),
+                ("grid", ctypes.c_int), ("lam", ctypes.c_double),
+                ("tt_min", ctypes.c_double), ("tt_max", ctypes.c_double),
+                ("tt_step", ctypes.c_double), ("rmax", ctypes.c_double),
+                ("rstep", ctypes.c_double), ("hist", ctypes.c_int),
+                ("nspecies", ctypes.c_int),
+                ("sp", ctypes.POINTER(OrcSpecies)), ("natoms", ctypes.c_int64),
+                ("x", ctypes.POINTER(ctypes.c_float)),
+                ("y", ctypes.POINTER(ctypes.c_float)),
+                ("z", ctypes.POINTER(ctypes.c_float))]
+
+
+def read_deb(path):
+    """The oracle's .deb parser (orc_deb_read): (header dict, species list
+    of dicts, float32 [N, 3] coordinates); raises on a parse error."""
+    d = OrcDeb()
+    rc = lib().orc_deb_read(path.encode(), ctypes.byref(d))
+    if rc != 0:
+        raise RuntimeError("orc_deb_read(%s) = %d" % (path, rc))
+    try:
+        hdr = {k: getattr(d, k) for k in ("device", "block", "grid", "lam",
+                                          "tt_min", "tt_max", "tt_step",
+                                          "rmax", "rstep", "hist")}
+        sp = [{"n": d.sp[i].n, "name": d.sp[i].name.decode(),
+               "occ": d.sp[i].occ, "beq": d.sp[i].beq,
+               "a": list(d.sp[i].a), "b": list(d.sp[i].b), "c": d.sp[i].c}
+              for i in range(d.nspecies)]
+        n = d.natoms
+        xyz = np.empty((n, 3), np.float32)
+        for c, arr in enumerate((d.x, d.y, d.z)):
+            if n:
+                xyz[:, c] = np.ctypeslib.as_array(arr, shape=(n,))
+        return hdr, sp, xyz
+    finally:
+        lib().orc_deb_free(ctypes.byref(d))
 
 
 def _p(a, ct):

@@ -6,6 +6,9 @@ Reads the reference checkout (path given as the first argument, default
 * ``GammaAl2O3_10nm.deb.xz`` and ``UH3_7nm.deb.xz`` — the shipped example
   inputs, xz-compressed byte for byte (Data/GammaAl2O3_10nm.deb,
   Data/UH3_7nm.deb).
+* ``UH3_7nm.xyz.xz`` and ``UH3_7nm_reduced.xyz.xz`` — the shipped .xyz
+  sources of UH3_7nm.deb (six and four columns), from which the reference's
+  Matlab converter wrote that .deb (Data/UH3_7nm{,_reduced}.xyz).
 * ``golden.json`` — for every shipped output (the six
   Data/GammaAl2O3_10nm.debx<i>x<j> histograms and the .debI intensities of
   Gamma and UH3): the SHA-256 and line count of the file with its CRLF line
@@ -48,7 +51,8 @@ def describe(path, every):
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     data = os.path.join(ref, "Data")
-    for name in ("GammaAl2O3_10nm.deb", "UH3_7nm.deb"):
+    for name in ("GammaAl2O3_10nm.deb", "UH3_7nm.deb", "UH3_7nm.xyz",
+                 "UH3_7nm_reduced.xyz"):
         with open(os.path.join(data, name), "rb") as f:
             raw = f.read()
         with open(os.path.join(HERE, name + ".xz"), "wb") as f:

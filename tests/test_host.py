@@ -194,3 +194,52 @@ def test_packed_counter_bookkeeping():
                         glob[1] += 65536
         got = [(word & 0xFFFF) + glob[0], (word >> 16) + glob[1]]
         assert got == [int((bins == 0).sum()), int((bins == 1).sum())]
+
+
+def test_text_parser_matches_the_oracle_and_binary_form(golden_deb, tmp_path):
+    """The engine's .deb parser (whole-file scan, from_chars) gives the
+    oracle's values bit for bit; its binary form (dbx_deb_pack) round-trips
+    them, and packing the binary form again gives the same bytes."""
+    from oracle import pyoracle as orc
+    for key in ("Gamma", "UH3"):
+        src = golden_deb[key]
+        hdr, sp, xyz = orc.read_deb(src)
+        b1 = cd.deb_pack(src, str(tmp_path / (key + ".debb")))
+        d = cd.read_debb(b1)
+        assert (d.device, d.block, d.grid, d.hist) == (
+            hdr["device"], hdr["block"], hdr["grid"], hdr["hist"])
+        assert (d.lam, d.tt_min, d.tt_max, d.tt_step, d.rmax, d.rstep) == (
+            hdr["lam"], hdr["tt_min"], hdr["tt_max"], hdr["tt_step"],
+            hdr["rmax"], hdr["rstep"])
+        assert d.counts == [s["n"] for s in sp]
+        assert d.names == [s["name"] for s in sp]
+        for got, want in zip(d.species, sp):
+            assert got.occ == want["occ"] and got.beq == want["beq"]
+            assert list(got.a) == want["a"] and list(got.b) == want["b"]
+            assert got.c == want["c"]
+        assert d.xyz.dtype == np.float32
+        np.testing.assert_array_equal(d.xyz.view(np.uint32), xyz.view(np.uint32))
+        b2 = cd.deb_pack(b1, str(tmp_path / (key + "2.debb")))
+        assert open(b1, "rb").read() == open(b2, "rb").read()
+
+
+def test_parser_edge_cases(tmp_path):
+    p = tmp_path / "e.deb"
+    p.write_text("0 8 1024\n1.5 10 20 0.1\n10 0.01 2\n2\n"
+                 "1 O 1 0 1 1 1 1 1 1 1 1 1 1 0\n2 Al 1 0 1 1 1 1 1 1 1 1 1 1 0\n"
+                 "\n  \r\n+1.5 -0 1e-3\r\n\t0.1 0.2 0.3\n\n7 8 9   \n")
+    d = cd.read_debb(cd.deb_pack(str(p), str(tmp_path / "e.debb")))
+    assert d.counts == [1, 2]
+    np.testing.assert_array_equal(
+        d.xyz, np.array([[1.5, -0.0, 1e-3], [0.1, 0.2, 0.3], [7, 8, 9]], np.float32))
+    assert np.signbit(d.xyz[0, 1])
+    p.write_text("0 8 1024\n1.5 10 20 0.1\n10 0.01 0\n1\n"
+                 "2 O 1 0 1 1 1 1 1 1 1 1 1 1 0\n1 2 3\n")
+    with pytest.raises(cd.DebyeError) as e:
+        cd.deb_pack(str(p), str(tmp_path / "f.debb"))
+    assert e.value.code == -6  # count mismatch
+    p.write_text("0 8 1024\n1.5 10 20 0.1\n10 0.01 0\n1\n"
+                 "1 O 1 0 1 1 1 1 1 1 1 1 1 1 0\n1 x 3\n")
+    with pytest.raises(cd.DebyeError) as e:
+        cd.deb_pack(str(p), str(tmp_path / "g.debb"))
+    assert e.value.code == -5
