@@ -254,6 +254,79 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, check=8, plain_models=None):
     }
 
 
+def io_bench(eng, nfiles=16, seed=8):
+    """The file surface: (a) the reference's shipped Gamma-Al2O3 input
+    (117,936 atoms, rstep 1e-4, hist 2: six .debx files and the .debI) run
+    by the command line from its text and its binary form, and in-process
+    (dbx_run_deb, context already open); the reference logged 2.191 s to
+    load this file and 11.563 s for histograms, checks, .debx writing and
+    the Debye sum on a GTX 980 Ti (Data/cmd-logfile.txt:94, :500-501).
+    (b) A directory of `nfiles` small models (2k-20k atoms, hist 0): the
+    directory driver (dbx_run_dir, batched) against one command-line
+    process per file, which is how the reference's multisim runs them."""
+    import lzma
+    import shutil
+    import subprocess
+    import tempfile
+    import cudebye_gb300 as cd
+    from cudebye_gb300 import lattice
+    out = {}
+    tmp = tempfile.mkdtemp(prefix="dbx_io_")
+    try:
+        src = os.path.join(tmp, "Gamma.deb")
+        with open(os.path.join(ROOT, "tests", "golden",
+                               "GammaAl2O3_10nm.deb.xz"), "rb") as f:
+            raw = lzma.decompress(f.read())
+        with open(src, "wb") as f:
+            f.write(raw)
+        t0 = time.perf_counter()
+        cd.deb_pack(src, os.path.join(tmp, "Gamma.debb"))
+        out["pack_s"] = time.perf_counter() - t0
+        for form, path in (("text", src), ("binary", os.path.join(tmp, "Gamma.debb"))):
+            ts = []
+            for _ in range(2):
+                t0 = time.perf_counter()
+                r = subprocess.run([cd.CLI_PATH, path, "--out",
+                                    os.path.join(tmp, "o_" + form), "--quiet"],
+                                   capture_output=True, text=True)
+                ts.append(time.perf_counter() - t0)
+                if r.returncode != 0:
+                    raise RuntimeError(r.stderr)
+            out["cli_gamma_%s_s" % form] = min(ts)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            eng.run_deb(src, os.path.join(tmp, "o_inproc"))
+            ts.append(time.perf_counter() - t0)
+        out["run_deb_gamma_s"] = min(ts)
+        out["reference_logged_gamma_s"] = {"load": 2.191, "compute_and_write": 11.563,
+                                           "gpu": "GTX 980 Ti"}
+        d = os.path.join(tmp, "dir")
+        os.mkdir(d)
+        rng = np.random.default_rng(seed)
+        for i in range(nfiles):
+            lattice.random_model(rng, 2000, 20000, lattice.GRID_CU, "f%d" % i,
+                                 seed).write_deb(os.path.join(d, "f%02d.deb" % i))
+        t0 = time.perf_counter()
+        eng.run_dir(d)
+        out["dir_driver_s"] = time.perf_counter() - t0
+        for f in os.listdir(d):
+            if f.endswith("I"):
+                os.remove(os.path.join(d, f))
+        t0 = time.perf_counter()
+        for f in sorted(os.listdir(d)):
+            r = subprocess.run([cd.CLI_PATH, os.path.join(d, f), "--quiet"],
+                               capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(r.stderr)
+        out["cli_per_file_s"] = time.perf_counter() - t0
+        out["files"] = nfiles
+        out["dir_speedup"] = out["cli_per_file_s"] / out["dir_driver_s"]
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return out
+
+
 def serving_bench(rates=(5, 20, 50, 100, 200), seconds=6.0, pool=32, seed=4):
     """The serving form: Poisson arrivals at each rate for `seconds`; each
     request is a spherical lattice model of 1,000-200,000 atoms
@@ -503,6 +576,8 @@ def run_engine(args):
                                          "sample")}
     if not args.no_batch:
         line["batch256"] = batch_bench(eng, plain_models=args.plain_models)
+    if not args.no_io:
+        line["file_io"] = io_bench(eng)
     model.free()
     eng.close()
     if not args.no_serve:
@@ -528,6 +603,8 @@ def main():
                     help="models of the batch timed in the plain form")
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the serving run")
+    ap.add_argument("--no-io", action="store_true",
+                    help="skip the file-surface timings")
     ap.add_argument("--serve-seconds", type=float, default=6.0,
                     help="seconds of Poisson arrivals per rate")
     args = ap.parse_args()
