@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -19,6 +20,48 @@ static uint32_t spread10(uint32_t v) {
   return v;
 }
 
+// One species: Morton order of its atoms on a (2^bits)^3 grid over the
+// model's bounding cube (stable LSD radix sort in passes of up to 11 bits:
+// atoms with equal codes keep their input order), written to atoms[start..).
+static void sort_species(const float *const xyz[3], int64_t start, int64_t n,
+                         const float lo[3], float scale, int bits,
+                         float4 *atoms) {
+  std::vector<uint32_t> code(n), code2(n);
+  std::vector<int32_t> idx(n), idx2(n);
+  const float top = (float)((1u << bits) - 1);
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t q[3];
+    for (int d = 0; d < 3; ++d) {
+      float t = (xyz[d][start + i] - lo[d]) * scale;
+      t = t >= 0.f ? (t <= top ? t : top) : 0.f;  // NaN -> 0
+      q[d] = (uint32_t)t;
+    }
+    code[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+    idx[i] = (int32_t)i;
+  }
+  const int total = 3 * bits;
+  const int passes = (total + 10) / 11;
+  const int width = (total + passes - 1) / passes;
+  std::vector<int64_t> hist((size_t(1) << width) + 1);
+  for (int shift = 0; shift < total; shift += width) {
+    const uint32_t mask = (1u << width) - 1u;
+    std::fill(hist.begin(), hist.end(), 0);
+    for (int64_t i = 0; i < n; ++i) ++hist[((code[i] >> shift) & mask) + 1];
+    for (size_t k = 0; k + 1 < hist.size(); ++k) hist[k + 1] += hist[k];
+    for (int64_t i = 0; i < n; ++i) {
+      const int64_t o = hist[(code[i] >> shift) & mask]++;
+      code2[o] = code[i];
+      idx2[o] = idx[i];
+    }
+    code.swap(code2);
+    idx.swap(idx2);
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t src = start + idx[i];
+    atoms[start + i] = make_float4(xyz[0][src], xyz[1][src], xyz[2][src], 0.f);
+  }
+}
+
 Error model_prepare(const float *x, const float *y, const float *z,
                     const int64_t *counts, int nspecies, Model *m,
                     std::vector<float4> *atoms_out) {
@@ -32,8 +75,10 @@ Error model_prepare(const float *x, const float *y, const float *z,
   if (natoms >= (int64_t(1) << 31)) return fail(DBX_ERR_ARG, "more than 2^31 atoms");
   m->nspecies = nspecies;
   m->natoms = natoms;
-  // Morton order on a 1024^3 grid over the model's bounding cube, per
-  // species, then tiles of kTile atoms with their bounding boxes.
+  // Morton order per species on a grid over the model's bounding cube with
+  // about 2 cells per atom (between 16^3 and 1024^3 cells), then tiles of
+  // kTile atoms with their bounding boxes. Any order gives the same
+  // histograms; a compact one gives tile pairs narrow distance ranges.
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   const float *xyz[3] = {x, y, z};
   for (int64_t i = 0; i < natoms; ++i)
@@ -44,12 +89,27 @@ Error model_prepare(const float *x, const float *y, const float *z,
     }
   float ext = 0;
   for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
-  const double scale = ext > 0 ? 1023.0 / ext : 0.0;
+  int bits = 4;
+  while (bits < 10 && (int64_t(1) << (3 * bits)) < 2 * natoms) ++bits;
+  const float scale = ext > 0 ? (float)((1u << bits) - 1) / ext : 0.f;
   std::vector<float4> &atoms = *atoms_out;
-  atoms.assign(std::max<int64_t>(natoms, 1), make_float4(0, 0, 0, 0));
-  std::vector<uint32_t> code, code2;
-  std::vector<int32_t> idx, idx2;
-  int64_t start = 0;
+  atoms.resize(std::max<int64_t>(natoms, 1));
+  atoms[0] = make_float4(0, 0, 0, 0);
+  std::vector<int64_t> start(nspecies + 1, 0);
+  for (int s = 0; s < nspecies; ++s) start[s + 1] = start[s] + counts[s];
+  // species sort independently: large models use one host thread each
+  if (natoms >= 65536 && nspecies > 1) {
+    std::vector<std::thread> th;
+    for (int s = 0; s < nspecies; ++s)
+      if (counts[s] > 0)
+        th.emplace_back(sort_species, xyz, start[s], counts[s], lo, scale, bits,
+                        atoms.data());
+    for (std::thread &t : th) t.join();
+  } else {
+    for (int s = 0; s < nspecies; ++s)
+      if (counts[s] > 0)
+        sort_species(xyz, start[s], counts[s], lo, scale, bits, atoms.data());
+  }
   m->tile_start.assign(1, 0);
   m->tiles.clear();
   m->boxes.clear();
@@ -57,50 +117,18 @@ Error model_prepare(const float *x, const float *y, const float *z,
   m->sp_count.clear();
   for (int s = 0; s < nspecies; ++s) {
     const int64_t n = counts[s];
-    // 30-bit Morton codes, then a stable LSD radix sort (three 10-bit
-    // passes): atoms with equal codes keep their input order.
-    code.resize(n);
-    code2.resize(n);
-    idx.resize(n);
-    idx2.resize(n);
-    for (int64_t i = 0; i < n; ++i) {
-      uint32_t q[3];
-      for (int d = 0; d < 3; ++d) {
-        double t = ((double)xyz[d][start + i] - lo[d]) * scale;
-        t = std::isfinite(t) ? std::min(std::max(t, 0.0), 1023.0) : 0.0;
-        q[d] = (uint32_t)t;
-      }
-      code[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
-      idx[i] = (int32_t)i;
-    }
-    for (int shift = 0; shift < 30; shift += 10) {
-      int64_t hist[1025] = {0};
-      for (int64_t i = 0; i < n; ++i) ++hist[((code[i] >> shift) & 1023u) + 1];
-      for (int b = 0; b < 1024; ++b) hist[b + 1] += hist[b];
-      for (int64_t i = 0; i < n; ++i) {
-        const int64_t o = hist[(code[i] >> shift) & 1023u]++;
-        code2[o] = code[i];
-        idx2[o] = idx[i];
-      }
-      code.swap(code2);
-      idx.swap(idx2);
-    }
-    for (int64_t i = 0; i < n; ++i) {
-      const int64_t src = start + idx[i];
-      atoms[start + i] = make_float4(x[src], y[src], z[src], 0.f);
-    }
-    m->sp_start.push_back(start);
+    m->sp_start.push_back(start[s]);
     m->sp_count.push_back(n);
     for (int64_t t0 = 0; t0 < n; t0 += kTile) {
       const int cnt = (int)std::min<int64_t>(kTile, n - t0);
-      m->tiles.push_back(make_int2((int)(start + t0), cnt));
+      m->tiles.push_back(make_int2((int)(start[s] + t0), cnt));
       TileBox b;
       for (int d = 0; d < 3; ++d) {
         b.lo[d] = INFINITY;
         b.hi[d] = -INFINITY;
       }
       for (int i = 0; i < cnt; ++i) {
-        const float4 a = atoms[start + t0 + i];
+        const float4 a = atoms[start[s] + t0 + i];
         const float v[3] = {a.x, a.y, a.z};
         for (int d = 0; d < 3; ++d) {
           b.lo[d] = std::min(b.lo[d], v[d]);
@@ -110,7 +138,6 @@ Error model_prepare(const float *x, const float *y, const float *z,
       m->boxes.push_back(b);
     }
     m->tile_start.push_back((int)m->tiles.size());
-    start += n;
   }
   return ok();
 }
