@@ -91,13 +91,14 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
   const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
   const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
   const unsigned uo = vo + base, ui = vi + base;
+  const f2 ninv = pk(-inv, -inv);
 #pragma unroll 2
   for (int j = 0; j < jend; ++j) {
     const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
     const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
     unsigned u[4], old[4];
-    bins2(X01, Y01, Z01, bx, by, bz, inv, 0u, u[0], u[1]);
-    bins2(X23, Y23, Z23, bx, by, bz, inv, 0u, u[2], u[3]);
+    bins2(X01, Y01, Z01, bx, by, bz, ninv, 0u, u[0], u[1]);
+    bins2(X23, Y23, Z23, bx, by, bz, ninv, 0u, u[2], u[3]);
     unsigned any = 0u;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -291,11 +292,19 @@ __global__ void plain_pairs_kernel(const float4 *__restrict__ atoms, long long a
     atomicAdd(oor, 1ull);
 }
 
-// Self-check of sqrt_rn against the IEEE square root for the floats with
-// bits in [lo, hi] (non-negative: hi <= bits of +inf). res[0] counts
-// mismatches, res[1] keeps the smallest mismatching bits. Inputs below
-// 2^-75 only need a result below 2^-37 (they bin to 0 either way); +inf only
-// a non-finite result.
+// Self-check of the kernels' square roots against the IEEE one for the
+// floats with bits in [lo, hi] (non-negative: hi <= bits of +inf): sqrt_rn,
+// and nsqrt2 (the packed form the tile kernels use) on the neighbouring
+// pair (u, u ^ 1) in its two lanes. res[0] counts mismatches, res[1] keeps
+// the smallest mismatching bits. Inputs below 2^-75 only need a result
+// below 2^-37 (they bin to 0 either way); +inf only a non-finite result.
+__device__ __forceinline__ bool sqrt_ok(float s, float a) {
+  const float b = __fsqrt_rn(s);
+  if (!(s >= 0x1p-75f)) return a < 0x1p-37f;
+  if (isinf(b)) return !isfinite(a);
+  return __float_as_uint(a) == __float_as_uint(b);
+}
+
 __global__ void check_sqrt_kernel(unsigned lo, unsigned hi,
                                   unsigned long long *res) {
   const unsigned long long n = (unsigned long long)(hi - lo) + 1ull;
@@ -305,14 +314,15 @@ __global__ void check_sqrt_kernel(unsigned lo, unsigned hi,
        i < n; i += stride) {
     const unsigned u = lo + (unsigned)i;
     const float s = __uint_as_float(u);
-    const float a = sqrt_rn(s), b = __fsqrt_rn(s);
-    bool good;
-    if (!(s >= 0x1p-75f))
-      good = a < 0x1p-37f;
-    else if (isinf(b))
-      good = !isfinite(a);
-    else
-      good = __float_as_uint(a) == __float_as_uint(b);
+    // the packed form on (u, partner); lane 0 holds u
+    const unsigned v = (u ^ 1u) <= 0x7F800000u ? (u ^ 1u) : u;
+    const float sv = __uint_as_float(v);
+    const f2 nc = sub2(pk(-0x1p-100f, -0x1p-100f), pk(s, sv));
+    float m0, m1;
+    upk(nsqrt2(nc), m0, m1);
+    const float c0 = __fadd_rn(s, 0x1p-100f);
+    const bool good = sqrt_ok(s, sqrt_rn(s)) && sqrt_ok(c0, -m0) &&
+                      sqrt_ok(__fadd_rn(sv, 0x1p-100f), -m1);
     if (!good) {
       atomicAdd(&res[0], 1ull);
       atomicMin(&res[1], (unsigned long long)u);

@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned long long *gh = out + kb;
   const unsigned lim = nbins - (unsigned)kb;
   const unsigned base = 0x4B000000u + (unsigned)kb;
+  const f2 ninv = pk(-inv, -inv);
   unsigned my_oor = 0;
   for (;;) {
     int idx = 0;
@@ -163,8 +164,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const float4 b = bj[j];
       const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
       unsigned old[4], lk[4];
-      bins2(X01, Y01, Z01, bx, by, bz, inv, base, lk[0], lk[1]);
-      bins2(X23, Y23, Z23, bx, by, bz, inv, base, lk[2], lk[3]);
+      bins2(X01, Y01, Z01, bx, by, bz, ninv, base, lk[0], lk[1]);
+      bins2(X23, Y23, Z23, bx, by, bz, ninv, base, lk[2], lk[3]);
       bool hit[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
