@@ -67,6 +67,7 @@ struct Req {
   int64_t model_out = 0;
   double t_submit = 0, t_done = 0;
   size_t offset = 0;  // of I in the lane's result buffer
+  bool solo = false;  // retried alone after its round failed
 };
 
 struct SModel {  // a resident model of the server
@@ -199,6 +200,7 @@ std::vector<Req *> admit(dbx_server *s) {
   const int64_t kMaxPairs = 40000000000LL;  // bounds a round's latency
   for (auto it = s->queue.begin(); it != s->queue.end() && out.size() < 64;) {
     Req *r = *it;
+    if (r->solo && !out.empty()) break;  // a retried request runs alone
     size_t need = 0;
     int nspecies = (int)r->counts.size();
     if (r->model) {
@@ -251,6 +253,7 @@ std::vector<Req *> admit(dbx_server *s) {
     if (r->model) s->models[r->model].busy = true;
     out.push_back(r);
     it = s->queue.erase(it);
+    if (r->solo) break;
   }
   return out;
 }
@@ -377,6 +380,38 @@ void finish_round(dbx_server *s, Lane &L, const Error &launch_err) {
   if (!e.code && L.hws.oor.p) e = hist_range_check(L.hws, L.stream);
   if (!e.code && L.tc.err.p) e = tc_check(&L.tc, L.stream);
   std::lock_guard<std::mutex> lock(s->mu);
+  // A failed round of several requests (one model with a distance beyond
+  // its rmax fails the shared histogram launch) is retried request by
+  // request, so that only the faulty one reports the error and the others'
+  // results do not depend on what they were batched with. A CUDA error is
+  // final for all.
+  const bool retry = e.code && e.code != DBX_ERR_CUDA && L.reqs.size() > 1;
+  for (auto it = L.reqs.rbegin(); retry && it != L.reqs.rend(); ++it) {
+    Req *r = *it;
+    const int64_t id = r->model ? r->model : r->model_out;
+    auto mit = s->models.find(id);
+    if (mit != s->models.end()) {
+      SModel &sm = mit->second;
+      sm.busy = false;
+      if (r->kind == kNewGrid) sm.K.clear();  // its row sums are recomputed
+      if (r->kind == kNew) {
+        s->used -= sm.bytes();
+        model_release(sm.m.get());
+        release(&sm.S);
+        s->models.erase(mit);
+      }
+    }
+    r->model_out = 0;
+    r->solo = true;
+    s->queue.push_front(r);  // reverse walk: the round's order is kept
+  }
+  if (retry) {
+    L.reqs.clear();
+    L.busy = false;
+    ++s->rounds;
+    s->cv_work.notify_all();
+    return;
+  }
   for (Req *r : L.reqs) {
     const int64_t id = r->model ? r->model : r->model_out;
     auto mit = s->models.find(id);

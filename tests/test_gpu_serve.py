@@ -135,3 +135,34 @@ def test_admission_by_hbm_budget(orc):
         with pytest.raises(cd.DebyeError) as e:
             run(srv)
         assert e.value.code == -3
+
+
+def test_a_failing_request_does_not_fail_its_round(orc):
+    """A request whose model has a distance beyond its rmax fails only
+    itself: the round it shared is redone request by request, and the
+    others' results are exact."""
+    good = make_requests(55, 5, nmin=500, nmax=1500)
+    bad = make_requests(56, 1, nmin=500, nmax=1500)[0]
+    with cd.Server(0) as srv:
+        tickets = []
+        for i, m in enumerate(good):
+            if i == 2:  # too few bins: distances beyond rmax
+                K = bad.k_grid()[1]
+                tickets.append((srv.submit(bad.species, bad.rstep, bad.nbins // 4,
+                                           K, xyz=bad.xyz, counts=bad.counts),
+                                len(K)))
+            K = m.k_grid()[1]
+            tickets.append((srv.submit(m.species, m.rstep, m.nbins, K,
+                                       xyz=m.xyz, counts=m.counts), len(K)))
+        results = []
+        for t, nq in tickets:
+            try:
+                results.append(srv.wait(t, nq))
+            except cd.DebyeError as e:
+                results.append(e)
+        assert isinstance(results[2], cd.DebyeError) and results[2].code == -7
+        ok = [r for i, r in enumerate(results) if i != 2]
+        for m, (I, mid, _) in zip(good, ok):
+            want = oracle_I(orc, m, m.k_grid()[1])
+            assert np.max(np.abs(I - want) / np.abs(want)) <= 1e-6
+        assert srv.stats()["completed"] == len(tickets)
