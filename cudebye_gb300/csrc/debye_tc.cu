@@ -25,12 +25,14 @@
 // per-chunk scale, the twiddle (double-float) and the chunk sum, and the
 // pair and q sums run in FP64.
 //
-// Kernel shape: CTA tile 128 rows x 64 columns, K = 256 in four slabs of
-// 64; operands are stored pre-tiled in global memory in the canonical
-// no-swizzle K-major core-matrix layout, so each slab is two contiguous
-// bulk copies (TMA engine, cp.async.bulk) completing on an mbarrier; one
-// thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> f32, M=128, N=64,
-// K=16) and commits to a second mbarrier; TMEM holds 4 x 64 f32 columns.
+// Kernel shape: tiles of 128 rows x 64 columns, K = 256 in four slabs of 64
+// stored pre-tiled in global memory in the canonical no-swizzle K-major
+// core-matrix layout, so each slab is two contiguous bulk copies (TMA
+// engine, cp.async.bulk) completing on an mbarrier. A persistent CTA per SM
+// runs three roles: a producer thread streams slabs through two stages, an
+// MMA thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> f32, M=128,
+// N=64, K=16) into one of two TMEM accumulator sets (4 classes x 64 f32
+// columns each) and commits, four epilogue warps drain the other set.
 // Every wait is bounded and reports a timeout through an error word.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -55,9 +57,7 @@ constexpr int kABlock = kTM * kKS;  // elements per digit per slab (16 KB)
 constexpr int kBBlock = kTN * kKS;  // 8 KB
 constexpr int kASlabBytes = kND * kABlock * 2;  // 64 KB
 constexpr int kBSlabBytes = kND * kBBlock * 2;  // 32 KB
-constexpr int kThreads = 128;
 constexpr int kTmemCols = 256;      // 4 classes x 64 columns
-constexpr int kSmemBytes = kASlabBytes + kBSlabBytes + 1024 + 64;
 constexpr double kSelfR = 0.0005;   // cuDebye-v15.cu:508
 
 // Element offset of (row, k) inside a [rows x 64] block stored as 8x8
@@ -248,157 +248,237 @@ __device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
                : "memory");
 }
 
-__global__ void __launch_bounds__(kThreads, 2)
-    gemm_kernel(const __nv_bfloat16 *__restrict__ A,
-                const __nv_bfloat16 *__restrict__ W,
-                const TcTile *__restrict__ tiles, const int *__restrict__ Ecol,
-                const float4 *__restrict__ tw, int Qp, int nrt,
-                double *__restrict__ P, int *__restrict__ err) {
+// ---- persistent, warp-specialised contraction ------------------------------
+// One CTA per SM loops over tiles t = blockIdx.x + i * gridDim.x (row tile
+// t % nrt, column tile t / nrt). Roles: warp 0 lane 0 streams the slabs of
+// A and W through kPStages shared-memory stages (bulk copies on the TMA
+// engine); warp 1 lane 0 issues the MMAs of a tile into one of two TMEM
+// accumulator sets (2 x 256 columns); warps 4-7 (TMEM lanes 0-127) run the
+// epilogue of the previous tile meanwhile. mbarriers: full[s] (copy landed),
+// empty[s] (MMAs on stage s done), accf[b] (accumulator set b complete),
+// acce[b] (set b drained by the epilogue). Every wait is bounded; a role that
+// times out records the error and stops, and the others then time out too.
+constexpr int kPThreads = 256;
+constexpr int kPStages = 2;
+constexpr int kPStageBytes = kASlabBytes + kBSlabBytes;
+constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
+
+// Epilogue of one tile for TMEM lane `row` (0..127) of accumulator set at
+// column offset acc_col: D = acc0 + acc1 2^-8 + acc2 2^-16 + acc3 2^-24,
+// scaled, rotated by the chunk twiddle and summed over the tile's 64 chunks.
+__device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
+                                                int mt, int nt,
+                                                const TcTile *__restrict__ tiles,
+                                                const int *__restrict__ Ecol,
+                                                const float4 *__restrict__ tw,
+                                                int Qp) {
+  const TcTile tile = tiles[nt];
+  const int m = mt * kTM + row;
+  const bool sinrow = m >= Qp;
+  const int q = sinrow ? m - Qp : m;
+  const float4 *twq = tw + q;
+  const int *E = Ecol + nt * kTN;
+  float sh = 0.f, sl = 0.f;
+#pragma unroll 1
+  for (int cg = 0; cg < kTN / 16; ++cg) {
+    uint32_t a0[16], a1[16], a2[16], a3[16];
+    tmem_ld16(lane_base + 0 * kTN + cg * 16, a0);
+    tmem_ld16(lane_base + 1 * kTN + cg * 16, a1);
+    tmem_ld16(lane_base + 2 * kTN + cg * 16, a2);
+    tmem_ld16(lane_base + 3 * kTN + cg * 16, a3);
+    tmem_wait16(a0);
+    tmem_wait16(a1);
+    tmem_wait16(a2);
+    tmem_wait16(a3);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int n = cg * 16 + i;
+      // exact two-sum of the top two classes, the rest rounded once
+      const float c0 = __uint_as_float(a0[i]);
+      const float c1 = __uint_as_float(a1[i]) * 0x1p-8f;
+      const float hi = c0 + c1;
+      const float hb = hi - c0;
+      const float lo = ((c0 - (hi - hb)) + (c1 - hb)) +
+                       fmaf(__uint_as_float(a2[i]), 0x1p-16f,
+                            __uint_as_float(a3[i]) * 0x1p-24f);
+      const float4 t = twq[(size_t)(tile.ch0 + n) * Qp];
+      const float th = sinrow ? t.z : t.x;
+      const float tl = sinrow ? t.w : t.y;
+      // (th + tl) * (hi + lo) as a double-float, scaled by 2^(E-14)
+      float p = th * hi;
+      float pe = fmaf(th, hi, -p);
+      pe = fmaf(th, lo, fmaf(tl, hi, pe));
+      const float sc = __int_as_float((__ldg(&E[n]) - 14 + 127) << 23);
+      p *= sc;
+      pe *= sc;
+      const float s = sh + p;
+      const float bb = s - sh;
+      const float e2 = (sh - (s - bb)) + (p - bb);
+      sl += e2 + pe;
+      sh = s + sl;
+      sl = sl - (sh - s);
+    }
+  }
+  return (double)sh + (double)sl;
+}
+
+__global__ void __launch_bounds__(kPThreads, 1)
+    gemm_persistent_kernel(const __nv_bfloat16 *__restrict__ A,
+                           const __nv_bfloat16 *__restrict__ W,
+                           const TcTile *__restrict__ tiles,
+                           const int *__restrict__ Ecol,
+                           const float4 *__restrict__ tw, int Qp, int nrt,
+                           int ntiles, double *__restrict__ P,
+                           int *__restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   uint8_t *sbase = smem_raw + (base - raw);
-  const uint32_t sA = base, sB = base + kASlabBytes;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(sbase + kASlabBytes + kBSlabBytes);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
-  __shared__ int s_E[kTN];
-  __shared__ int s_fail;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sbase + kPStages * kPStageBytes);
+  // bars: full[kPStages], empty[kPStages], accf[2], acce[2]
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * kPStages + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int mt = blockIdx.x % nrt, nt = blockIdx.x / nrt;
-  const uint32_t bar_load = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  auto bar = [&](int i) { return smem_u32(&bars[i]); };
+  const int FULL = 0, EMPTY = kPStages, ACCF = 2 * kPStages, ACCE = 2 * kPStages + 2;
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_load));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_mma));
+    for (int i = 0; i < 2 * kPStages + 2; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(i)));
+    for (int b = 0; b < 2; ++b)  // one arrival per epilogue warp
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(bar(ACCE + b)));
     asm volatile("fence.mbarrier_init.release.cluster;");
-    s_fail = 0;
   }
-  if (tid < kTN) s_E[tid] = Ecol[nt * kTN + tid];
   if (warp == 0) {
     asm volatile(
         "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
             smem_u32(tslot)),
-        "r"(kTmemCols));
+        "r"(2 * kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tslot;
+  const int total = nrt * ntiles;
 
-  if (tid == 0) {
-    constexpr uint32_t idesc = make_idesc(kTM, kTN);
-    const char *gA = reinterpret_cast<const char *>(A) +
-                     (size_t)mt * kNSlab * kASlabBytes;
-    const char *gW = reinterpret_cast<const char *>(W) +
-                     (size_t)nt * kNSlab * kBSlabBytes;
+  if (warp == 0 && lane == 0) {
+    // producer
+    int it = 0;
     bool ok = true;
-    for (int ks = 0; ks < kNSlab && ok; ++ks) {
-      asm volatile(
-          "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_load),
-          "r"(kASlabBytes + kBSlabBytes)
-          : "memory");
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-          "[%0], [%1], %2, [%3];" ::"r"(sA),
-          "l"(gA + (size_t)ks * kASlabBytes), "r"(kASlabBytes), "r"(bar_load)
-          : "memory");
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-          "[%0], [%1], %2, [%3];" ::"r"(sB),
-          "l"(gW + (size_t)ks * kBSlabBytes), "r"(kBSlabBytes), "r"(bar_load)
-          : "memory");
-      if (!mbar_wait(bar_load, ks & 1)) {
+    for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+      const int mt = t % nrt, nt = t / nrt;
+      const char *gA = reinterpret_cast<const char *>(A) +
+                       (size_t)mt * kNSlab * kASlabBytes;
+      const char *gW = reinterpret_cast<const char *>(W) +
+                       (size_t)nt * kNSlab * kBSlabBytes;
+      for (int ks = 0; ks < kNSlab; ++ks, ++it) {
+        const int st = it % kPStages, use = it / kPStages;
+        if (use > 0 && !mbar_wait(bar(EMPTY + st), (use - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        const uint32_t sA = base + st * kPStageBytes, sB = sA + kASlabBytes;
+        asm volatile(
+            "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                bar(FULL + st)),
+            "r"(kPStageBytes)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+            "[%0], [%1], %2, [%3];" ::"r"(sA),
+            "l"(gA + (size_t)ks * kASlabBytes), "r"(kASlabBytes), "r"(bar(FULL + st))
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+            "[%0], [%1], %2, [%3];" ::"r"(sB),
+            "l"(gW + (size_t)ks * kBSlabBytes), "r"(kBSlabBytes), "r"(bar(FULL + st))
+            : "memory");
+      }
+    }
+    if (!ok) atomicExch(err, 1);
+    // let the copies still in flight land before the CTA can exit
+    for (int k = it > kPStages ? it - kPStages : 0; k < it; ++k)
+      mbar_wait(bar(FULL + k % kPStages), (k / kPStages) & 1);
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = make_idesc(kTM, kTN);
+    int it = 0, tc = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++tc) {
+      const int b = tc & 1, ub = tc >> 1;
+      if (ub > 0 && !mbar_wait(bar(ACCE + b), (ub - 1) & 1)) {
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t acc_base = tmem + b * kTmemCols;
+      for (int ks = 0; ks < kNSlab; ++ks, ++it) {
+        const int st = it % kPStages, use = it / kPStages;
+        if (!mbar_wait(bar(FULL + st), use & 1)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t sA = base + st * kPStageBytes, sB = sA + kASlabBytes;
 #pragma unroll
-      for (int w = 0; w < 4; ++w) {
+        for (int w = 0; w < 4; ++w) {
 #pragma unroll
-        for (int s = 0; s <= w; ++s) {
-          const int t = w - s;
+          for (int s = 0; s <= w; ++s) {
+            const int u = w - s;
 #pragma unroll
-          for (int kk = 0; kk < kKS / 16; ++kk) {
-            const uint64_t ad = make_desc(sA + s * kABlock * 2 + kk * 256, 128, 1024);
-            const uint64_t bd = make_desc(sB + t * kBBlock * 2 + kk * 256, 128, 1024);
-            const uint32_t acc = (ks > 0 || s > 0 || kk > 0) ? 1u : 0u;
-            mma_bf16(tmem + w * kTN, ad, bd, idesc, acc);
+            for (int kk = 0; kk < kKS / 16; ++kk) {
+              const uint64_t ad = make_desc(sA + s * kABlock * 2 + kk * 256, 128, 1024);
+              const uint64_t bd = make_desc(sB + u * kBBlock * 2 + kk * 256, 128, 1024);
+              const uint32_t acc = (ks > 0 || s > 0 || kk > 0) ? 1u : 0u;
+              mma_bf16(acc_base + w * kTN, ad, bd, idesc, acc);
+            }
           }
         }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
+            "[%0];" ::"r"(bar(EMPTY + st))
+            : "memory");
       }
+      if (!ok) break;
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
-          "[%0];" ::"r"(bar_mma)
+          "[%0];" ::"r"(bar(ACCF + b))
           : "memory");
-      if (!mbar_wait(bar_mma, ks & 1)) ok = false;
     }
-    if (!ok) {
-      s_fail = 1;
-      atomicExch(err, 1);
+    if (!ok) atomicExch(err, 1);
+    // the MMAs issued so far finish before the CTA can exit
+    if (it > 0) {
+      const int k = it - 1;
+      mbar_wait(bar(EMPTY + k % kPStages), (k / kPStages) & 1);
     }
-  }
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-
-  if (!s_fail) {
-    // Epilogue: row = TMEM lane; sum the 64 chunks of this tile.
-    const TcTile tile = tiles[nt];
-    const int row = warp * 32 + lane;
-    const int m = mt * kTM + row;
-    const bool sinrow = m >= Qp;
-    const int q = sinrow ? m - Qp : m;
-    const float4 *twq = tw + q;
-    float sh = 0.f, sl = 0.f;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-    for (int cg = 0; cg < kTN / 16; ++cg) {
-      uint32_t a0[16], a1[16], a2[16], a3[16];
-      tmem_ld16(lane_base + 0 * kTN + cg * 16, a0);
-      tmem_ld16(lane_base + 1 * kTN + cg * 16, a1);
-      tmem_ld16(lane_base + 2 * kTN + cg * 16, a2);
-      tmem_ld16(lane_base + 3 * kTN + cg * 16, a3);
-      tmem_wait16(a0);
-      tmem_wait16(a1);
-      tmem_wait16(a2);
-      tmem_wait16(a3);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int n = cg * 16 + i;
-        // D = acc0 + acc1 2^-8 + acc2 2^-16 + acc3 2^-24 (exact integers):
-        // exact two-sum of the top two classes, the rest rounded once.
-        const float c0 = __uint_as_float(a0[i]);
-        const float c1 = __uint_as_float(a1[i]) * 0x1p-8f;
-        const float hi = c0 + c1;
-        const float hb = hi - c0;
-        const float lo = ((c0 - (hi - hb)) + (c1 - hb)) +
-                         fmaf(__uint_as_float(a2[i]), 0x1p-16f,
-                              __uint_as_float(a3[i]) * 0x1p-24f);
-        const float4 t = twq[(size_t)(tile.ch0 + n) * Qp];
-        const float th = sinrow ? t.z : t.x;
-        const float tl = sinrow ? t.w : t.y;
-        // (th + tl) * (hi + lo) as a double-float, scaled by 2^(E-14)
-        float p = th * hi;
-        float pe = fmaf(th, hi, -p);
-        pe = fmaf(th, lo, fmaf(tl, hi, pe));
-        const float sc = __int_as_float((s_E[n] - 14 + 127) << 23);
-        p *= sc;
-        pe *= sc;
-        const float s = sh + p;
-        const float bb = s - sh;
-        const float e2 = (sh - (s - bb)) + (p - bb);
-        sl += e2 + pe;
-        sh = s + sl;
-        sl = sl - (sh - s);
+  } else if (warp >= 4) {
+    // epilogue: warp 4 + i reads TMEM lanes 32 i .. 32 i + 31
+    const int row = (warp - 4) * 32 + lane;
+    int tc = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++tc) {
+      const int b = tc & 1, ub = tc >> 1;
+      const int mt = t % nrt, nt = t / nrt;
+      if (!mbar_wait(bar(ACCF + b), ub & 1)) {
+        atomicExch(err, 1);
+        break;
       }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t lane_base =
+          tmem + b * kTmemCols + ((uint32_t)((warp - 4) * 32) << 16);
+      P[(size_t)nt * (2 * Qp) + mt * kTM + row] =
+          tile_epilogue(lane_base, row, mt, nt, tiles, Ecol, tw, Qp);
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar(ACCE + b))
+                     : "memory");
     }
-    P[(size_t)nt * (2 * Qp) + m] = (double)sh + (double)sl;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0)
     asm volatile(
         "tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-        "r"(kTmemCols));
+        "r"(2 * kTmemCols));
 }
 
 // I[model][q] = sum over the model's columns (pair order) of
@@ -546,9 +626,14 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
                                sizeof(int) * (nmodels + 1), cudaMemcpyHostToDevice,
                                stream));
   st->h2d += sizeof(TcTile) * ntiles + sizeof(TcCol) * ncols + sizeof(int) * (nmodels + 1);
-  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_kernel,
+  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kSmemBytes));
+                                    kPSmemBytes));
+  if (!st->num_sms) {
+    int dev = 0;
+    DBX_CUDA_TRY(cudaGetDevice(&dev));
+    DBX_CUDA_TRY(cudaDeviceGetAttribute(&st->num_sms, cudaDevAttrMultiProcessorCount, dev));
+  }
   st->ncols = ncols;
   st->nmodels = nmodels;
   st->ntiles = ntiles;
@@ -572,10 +657,12 @@ Error tc_execute(TcState *st, const double *d_K, double *d_I,
       (__nv_bfloat16 *)st->W.p, (int *)st->E.p, (int *)st->nonself.p);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->start(DBX_T_DEBYE, stream);
-  gemm_kernel<<<nrt * ntiles, kThreads, kSmemBytes, stream>>>(
+  const int total = nrt * ntiles;
+  gemm_persistent_kernel<<<std::min(total, st->num_sms), kPThreads, kPSmemBytes,
+                           stream>>>(
       (const __nv_bfloat16 *)st->basis.p, (const __nv_bfloat16 *)st->W.p,
       (const TcTile *)st->tiles.p, (const int *)st->E.p, (const float4 *)st->twid.p,
-      Qp, nrt, (double *)st->P.p, (int *)st->err.p);
+      Qp, nrt, ntiles, (double *)st->P.p, (int *)st->err.p);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->stop(DBX_T_DEBYE, stream);
   dim3 rg((nq + 127) / 128, st->nmodels);

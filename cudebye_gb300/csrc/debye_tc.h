@@ -26,6 +26,7 @@ struct TcState {  // cached plan data (basis, twiddles) and workspace
   int64_t h2d = 0, d2h = 0;
   // shape of the prepared contraction
   int ncols = 0, nmodels = 0, ntiles = 0, nq = 0, Qp = 0;
+  int num_sms = 0;  // persistent contraction: one CTA per SM
   double rstep = 0;
   double *S_out = nullptr;  // optional: per-column row sums S[c][q]
 };
