@@ -539,10 +539,10 @@ def run_engine(args):
                           "sampled SM clock)" % (ops, sm_mhz)}
     flops = 2.0 * len(K) * m.nbins * npair_types
     tc_ach = flops / (ph["debye"] / 1e3) / 1e12
-    roof_tc = {"kernel": "debye (weights + gemm + reduce)", "bound": "tensor",
+    roof_tc = {"kernel": "gemm_persistent_kernel", "bound": "tensor",
                "achieved": tc_ach, "peak": pk["bf16_tflops"],
                "unit": "TFLOP/s", "frac": tc_ach / pk["bf16_tflops"],
-               "traffic": measured_traffic("gemm_kernel", m.label),
+               "traffic": measured_traffic("gemm_persistent_kernel", m.label),
                "flops_basis": "2 x q x bins x pair types (one FP64-exact "
                               "sinc product per count); the split form "
                               "issues 10 bf16 MMAs per product",
