@@ -129,6 +129,19 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_times(times, ws, device=None):
+    """Whole-job times of one replica per rank: the max over ranks of each
+    entry (the slowest replica ends the job)."""
+    if ws <= 1:
+        return [float(t) for t in times]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in times], dtype=torch.float64,
+                     device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -410,8 +423,8 @@ def run_reference(args):
         return 0
     m = workload()
     tt, K = m.k_grid()
-    for _ in range(args.warmup):
-        pass  # the CPU port has no warm-up effects worth a full sample
+    for _ in range(args.warmup):  # untimed samples: caches, page faults
+        cpu_baseline(m, K, threads=0)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -504,11 +517,7 @@ def run_engine(args):
         step_ms.append(a.elapsed_time(b))
     t_step = float(np.mean(step_ms)) / 1e3
     t_e2e = float(np.mean(e2e_s))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_step, t_e2e], device=local)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step, t_e2e = float(t[0]), float(t[1])
+    t_step, t_e2e = job_times([t_step, t_e2e], ws, device=local)
     if rank != 0:
         eng.close()
         return 0
