@@ -48,6 +48,10 @@ struct dbx_ctx {
   size_t used = 0;    // device bytes held
   cudaStream_t stream = nullptr;      // launch stream (own or caller's)
   cudaStream_t own_stream = nullptr;
+  float4 *pin = nullptr;              // pinned staging of model uploads
+  size_t pin_cap = 0;                 // in atoms
+  cudaEvent_t pin_ev = nullptr;       // the last upload's copy is done
+  bool pin_used = false;
   dbx::Timers tm;
   int64_t h2d = 0, d2h = 0;           // bytes copied (dbx_get_traffic)
   std::map<int64_t, std::unique_ptr<dbx::Model>> models;
@@ -564,6 +568,8 @@ int dbx_destroy(dbx_ctx *c) {
       cudaEventDestroy(p[0]);
       cudaEventDestroy(p[1]);
     }
+  if (c->pin_ev) cudaEventDestroy(c->pin_ev);
+  if (c->pin) cudaFreeHost(c->pin);
   cudaStreamDestroy(c->own_stream);
   delete c;
   return DBX_OK;
@@ -575,17 +581,44 @@ int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
   if (!c || !counts || nspecies < 1 || !model_id) return DBX_ERR_ARG;
   cudaSetDevice(c->device);
   auto m = std::make_unique<dbx::Model>();
-  std::vector<float4> atoms;
-  Error e = dbx::model_prepare(x, y, z, counts, nspecies, m.get(), &atoms);
+  int64_t natoms = 0;
+  for (int s = 0; s < nspecies; ++s) natoms += std::max<int64_t>(counts[s], 0);
+  // The sorted atoms are staged in pinned memory owned by the context, so
+  // the upload is an asynchronous copy; the staging buffer is reused only
+  // once the previous upload's copy has completed.
+  const size_t n = (size_t)std::max<int64_t>(natoms, 1);
+  if (c->pin_used) {
+    const cudaError_t ce = cudaEventSynchronize(c->pin_ev);
+    if (ce != cudaSuccess)
+      return set_err(c, dbx::fail(DBX_ERR_CUDA, cudaGetErrorString(ce)));
+    c->pin_used = false;
+  }
+  if (c->pin_cap < n) {
+    if (c->pin) cudaFreeHost(c->pin);
+    c->pin = nullptr;
+    c->pin_cap = 0;
+    if (cudaMallocHost((void **)&c->pin, n * sizeof(float4)) != cudaSuccess) {
+      c->pin = nullptr;
+      return set_err(c, dbx::fail(DBX_ERR_NOMEM, "pinned staging buffer"));
+    }
+    c->pin_cap = n;
+  }
+  if (!c->pin_ev &&
+      cudaEventCreateWithFlags(&c->pin_ev, cudaEventDisableTiming) != cudaSuccess)
+    return set_err(c, dbx::fail(DBX_ERR_CUDA, "cudaEventCreate failed"));
+  Error e = dbx::model_prepare(x, y, z, counts, nspecies, m.get(), c->pin);
   if (e.code) return set_err(c, e);
   const size_t need = dbx::model_upload_bytes(*m);
   if (c->budget && c->used + need > c->budget)
     return set_err(c, dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by model"));
-  e = dbx::model_to_device(m.get(), atoms, c->stream);
+  e = dbx::model_to_device(m.get(), c->pin, c->stream);
   if (e.code) {
     dbx::model_release(m.get());
     return set_err(c, e);
   }
+  if (cudaEventRecord(c->pin_ev, c->stream) != cudaSuccess)
+    return set_err(c, dbx::fail(DBX_ERR_CUDA, "cudaEventRecord failed"));
+  c->pin_used = true;
   c->used += m->dev_bytes;
   c->h2d += m->dev_bytes;
   m->id = c->next_id++;

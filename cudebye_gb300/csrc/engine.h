@@ -102,12 +102,14 @@ struct Model {
 
 // Model building (model.cu): host-side sort, tiles and boxes; device copy;
 // release.
+// atoms: room for max(natoms, 1) float4 (host memory, pinned or not).
 Error model_prepare(const float *x, const float *y, const float *z,
                     const int64_t *counts, int nspecies, Model *m,
-                    std::vector<float4> *atoms);
+                    float4 *atoms);
 size_t model_upload_bytes(const Model &m);
-Error model_to_device(Model *m, const std::vector<float4> &atoms,
-                      cudaStream_t stream);
+// Copies max(natoms, 1) atoms; from pinned memory the copy is asynchronous
+// and `atoms` must stay untouched until it completes on `stream`.
+Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream);
 size_t model_device_bytes(const Model &m);  // atoms, tiles, hist, plan
 void model_release(Model *m);
 

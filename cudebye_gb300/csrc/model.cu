@@ -20,15 +20,30 @@ static uint32_t spread10(uint32_t v) {
   return v;
 }
 
-// One species: Morton order of its atoms on a (2^bits)^3 grid over the
-// model's bounding cube (stable LSD radix sort in passes of up to 11 bits:
-// atoms with equal codes keep their input order), written to atoms[start..).
+// One species: Morton order of its atoms on a grid over the species'
+// bounding cube with about 2 cells per atom (16^3 to 1024^3 cells; stable
+// LSD radix sort in passes of up to 11 bits, so atoms with equal codes keep
+// their input order), written to atoms[start..start+n), and the bounding
+// boxes of its tiles of kTile atoms. Any order gives the same histograms; a
+// compact one gives tile pairs narrow distance ranges.
 static void sort_species(const float *const xyz[3], int64_t start, int64_t n,
-                         const float lo[3], float scale, int bits,
-                         float4 *atoms) {
+                         float4 *atoms, std::vector<TileBox> *boxes) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int d = 0; d < 3; ++d) {
+    const float *v = xyz[d] + start;
+    for (int64_t i = 0; i < n; ++i) {
+      lo[d] = std::min(lo[d], v[i]);
+      hi[d] = std::max(hi[d], v[i]);
+    }
+  }
+  float ext = 0;
+  for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
+  int bits = 4;
+  while (bits < 10 && (int64_t(1) << (3 * bits)) < 2 * n) ++bits;
+  const float top = (float)((1u << bits) - 1);
+  const float scale = ext > 0 ? top / ext : 0.f;  // NaN extent: scale NaN, t 0
   std::vector<uint32_t> code(n), code2(n);
   std::vector<int32_t> idx(n), idx2(n);
-  const float top = (float)((1u << bits) - 1);
   for (int64_t i = 0; i < n; ++i) {
     uint32_t q[3];
     for (int d = 0; d < 3; ++d) {
@@ -60,11 +75,29 @@ static void sort_species(const float *const xyz[3], int64_t start, int64_t n,
     const int64_t src = start + idx[i];
     atoms[start + i] = make_float4(xyz[0][src], xyz[1][src], xyz[2][src], 0.f);
   }
+  boxes->clear();
+  for (int64_t t0 = 0; t0 < n; t0 += kTile) {
+    const int cnt = (int)std::min<int64_t>(kTile, n - t0);
+    TileBox bx;
+    for (int d = 0; d < 3; ++d) {
+      bx.lo[d] = INFINITY;
+      bx.hi[d] = -INFINITY;
+    }
+    for (int i = 0; i < cnt; ++i) {
+      const float4 a = atoms[start + t0 + i];
+      const float v[3] = {a.x, a.y, a.z};
+      for (int d = 0; d < 3; ++d) {
+        bx.lo[d] = std::min(bx.lo[d], v[d]);
+        bx.hi[d] = std::max(bx.hi[d], v[d]);
+      }
+    }
+    boxes->push_back(bx);
+  }
 }
 
 Error model_prepare(const float *x, const float *y, const float *z,
                     const int64_t *counts, int nspecies, Model *m,
-                    std::vector<float4> *atoms_out) {
+                    float4 *atoms) {
   if (!counts || nspecies < 1) return fail(DBX_ERR_ARG, "need >= 1 species");
   int64_t natoms = 0;
   for (int s = 0; s < nspecies; ++s) {
@@ -75,40 +108,21 @@ Error model_prepare(const float *x, const float *y, const float *z,
   if (natoms >= (int64_t(1) << 31)) return fail(DBX_ERR_ARG, "more than 2^31 atoms");
   m->nspecies = nspecies;
   m->natoms = natoms;
-  // Morton order per species on a grid over the model's bounding cube with
-  // about 2 cells per atom (between 16^3 and 1024^3 cells), then tiles of
-  // kTile atoms with their bounding boxes. Any order gives the same
-  // histograms; a compact one gives tile pairs narrow distance ranges.
-  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   const float *xyz[3] = {x, y, z};
-  for (int64_t i = 0; i < natoms; ++i)
-    for (int d = 0; d < 3; ++d) {
-      const float v = xyz[d][i];
-      if (v < lo[d]) lo[d] = v;
-      if (v > hi[d]) hi[d] = v;
-    }
-  float ext = 0;
-  for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
-  int bits = 4;
-  while (bits < 10 && (int64_t(1) << (3 * bits)) < 2 * natoms) ++bits;
-  const float scale = ext > 0 ? (float)((1u << bits) - 1) / ext : 0.f;
-  std::vector<float4> &atoms = *atoms_out;
-  atoms.resize(std::max<int64_t>(natoms, 1));
   atoms[0] = make_float4(0, 0, 0, 0);
   std::vector<int64_t> start(nspecies + 1, 0);
   for (int s = 0; s < nspecies; ++s) start[s + 1] = start[s] + counts[s];
+  std::vector<std::vector<TileBox>> boxes(nspecies);
   // species sort independently: large models use one host thread each
   if (natoms >= 65536 && nspecies > 1) {
     std::vector<std::thread> th;
     for (int s = 0; s < nspecies; ++s)
       if (counts[s] > 0)
-        th.emplace_back(sort_species, xyz, start[s], counts[s], lo, scale, bits,
-                        atoms.data());
+        th.emplace_back(sort_species, xyz, start[s], counts[s], atoms, &boxes[s]);
     for (std::thread &t : th) t.join();
   } else {
     for (int s = 0; s < nspecies; ++s)
-      if (counts[s] > 0)
-        sort_species(xyz, start[s], counts[s], lo, scale, bits, atoms.data());
+      if (counts[s] > 0) sort_species(xyz, start[s], counts[s], atoms, &boxes[s]);
   }
   m->tile_start.assign(1, 0);
   m->tiles.clear();
@@ -119,24 +133,10 @@ Error model_prepare(const float *x, const float *y, const float *z,
     const int64_t n = counts[s];
     m->sp_start.push_back(start[s]);
     m->sp_count.push_back(n);
-    for (int64_t t0 = 0; t0 < n; t0 += kTile) {
-      const int cnt = (int)std::min<int64_t>(kTile, n - t0);
-      m->tiles.push_back(make_int2((int)(start[s] + t0), cnt));
-      TileBox b;
-      for (int d = 0; d < 3; ++d) {
-        b.lo[d] = INFINITY;
-        b.hi[d] = -INFINITY;
-      }
-      for (int i = 0; i < cnt; ++i) {
-        const float4 a = atoms[start[s] + t0 + i];
-        const float v[3] = {a.x, a.y, a.z};
-        for (int d = 0; d < 3; ++d) {
-          b.lo[d] = std::min(b.lo[d], v[d]);
-          b.hi[d] = std::max(b.hi[d], v[d]);
-        }
-      }
-      m->boxes.push_back(b);
-    }
+    for (int64_t t0 = 0; t0 < n; t0 += kTile)
+      m->tiles.push_back(make_int2((int)(start[s] + t0),
+                                   (int)std::min<int64_t>(kTile, n - t0)));
+    m->boxes.insert(m->boxes.end(), boxes[s].begin(), boxes[s].end());
     m->tile_start.push_back((int)m->tiles.size());
   }
   return ok();
@@ -147,15 +147,14 @@ size_t model_upload_bytes(const Model &m) {
          sizeof(int2) * std::max<size_t>(m.tiles.size(), 1);
 }
 
-Error model_to_device(Model *m, const std::vector<float4> &atoms,
-                      cudaStream_t stream) {
-  const size_t abytes = sizeof(float4) * atoms.size();
+Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream) {
+  const size_t abytes = sizeof(float4) * std::max<int64_t>(m->natoms, 1);
   const size_t tbytes = sizeof(int2) * std::max<size_t>(m->tiles.size(), 1);
   if (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
       cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess)
     return fail(DBX_ERR_NOMEM, "cudaMalloc failed for model");
   m->dev_bytes = abytes + tbytes;
-  DBX_CUDA_TRY(cudaMemcpyAsync(m->d_atoms, atoms.data(), abytes,
+  DBX_CUDA_TRY(cudaMemcpyAsync(m->d_atoms, atoms, abytes,
                                cudaMemcpyHostToDevice, stream));
   if (!m->tiles.empty())
     DBX_CUDA_TRY(cudaMemcpyAsync(m->d_tiles, m->tiles.data(),

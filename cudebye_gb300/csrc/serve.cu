@@ -269,10 +269,13 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
   for (Req *r : batch) {
     if (r->kind != kNew) continue;
     auto m = std::make_unique<Model>();
-    std::vector<float4> atoms;
+    int64_t natoms = 0;
+    for (int64_t c : r->counts) natoms += std::max<int64_t>(c, 0);
+    // pageable: the copy is staged before cudaMemcpyAsync returns
+    std::vector<float4> atoms(std::max<int64_t>(natoms, 1));
     DBX_TRY(model_prepare(r->x.data(), r->y.data(), r->z.data(), r->counts.data(),
-                          (int)r->counts.size(), m.get(), &atoms));
-    DBX_TRY(model_to_device(m.get(), atoms, st));
+                          (int)r->counts.size(), m.get(), atoms.data()));
+    DBX_TRY(model_to_device(m.get(), atoms.data(), st));
     m->hist_pitch = pitch_of(r->nbins);
     m->hist_bytes = hist_bytes(m->nspecies, r->nbins);
     DBX_CUDA_TRY(cudaMalloc(&m->d_hist, m->hist_bytes));
