@@ -215,10 +215,10 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, check=8, plain_models=None):
     histogram launch + one tensor-core contraction for all 256 models,
     CUDA-graph replay) and (b) the plain unbatched FP32 GPU form (model by
     model: one-thread-per-pair global-atomic histogram + FP32 direct Debye
-    sum). Max relative error of (a) against the FP64 oracle on `check`
-    sampled models (every 10th q)."""
+    sum). Max relative error of (a) against the FP64 direct sum on `check`
+    sampled models (every 10th q): the reference's arithmetic on the
+    device, which the tests hold within 1e-11 of the CPU FP64 oracle."""
     from cudebye_gb300 import lattice
-    from oracle import pyoracle as orc
     mods = lattice.batch256(seed=seed, nmodels=nmodels)
     tt, K = mods[0].k_grid()
     sp = [s for m in mods for s in m.species]
@@ -238,9 +238,9 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, check=8, plain_models=None):
         pick = sorted(rng.choice(len(mods), size=min(check, len(mods)),
                                  replace=False).tolist())
         worst = 0.0
-        for i in pick:
-            h = eng.histogram(hs[i], 1e-3, nb[i])  # resident from the pass
-            want = orc.intensity(K[::10], h, mods[i].species, 1e-3)
+        for i in pick:  # histograms resident from the pass
+            want = eng.intensity(hs[i], 1e-3, nb[i], mods[i].species,
+                                 K[::10], mode="fp64")
             worst = max(worst, float(np.max(np.abs(I[i, ::10] - want)
                                             / np.abs(want))))
         # plain form over a subset (it is slow), scaled per pattern
@@ -262,9 +262,56 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, check=8, plain_models=None):
         "speedup_batched_vs_plain": t_plain / t_tc,
         "ms_per_batch": t_tc * 1e3,
         "max_rel_err_vs_fp64": worst, "err_models_checked": len(pick),
+        "err_reference": "FP64 direct sum on the device (every 10th q)",
         "timing": "host wall clock around dbx_patterns (H2D species/K, graph "
                   "replay, D2H of all intensities), median of %d passes" % steps,
     }
+
+
+def precision_bench(eng, reps=3):
+    """The precision form: the spinel model's histograms (resident) summed
+    on the 20,000-point q grid (2theta 5-150 deg at 0.7107 A) by the exact
+    tensor-core split, the three-product BF16x3 form, the plain FP32
+    direct sum and the FP64 direct sum (the reference's arithmetic, the
+    error reference). Per form: device time of the Debye sum (CUDA events,
+    median of `reps`) and max relative error over all q."""
+    from cudebye_gb300 import lattice
+    m = lattice.precision()
+    tt, K = m.k_grid()
+    mod = eng.upload(m.xyz, m.counts)
+    res = {}
+    try:
+        eng.histogram(mod, m.rstep, m.nbins)
+        outs = {}
+        for mode in ("fp64", "tc", "tc3", "fp32"):
+            ts, ws = [], []
+            for _ in range(reps + 1):
+                t0 = time.perf_counter()
+                outs[mode] = eng.intensity(mod, m.rstep, m.nbins, m.species, K,
+                                           mode=mode)
+                ws.append(time.perf_counter() - t0)
+                ts.append(eng.timing()["debye"])
+            res[mode] = {"debye_kernel_ms": float(np.median(ts[1:])),
+                         "call_ms": float(np.median(ws[1:])) * 1e3}
+        ref = outs["fp64"]
+        for mode in ("tc", "tc3", "fp32"):
+            rel = np.abs(outs[mode] - ref) / np.abs(ref)
+            res[mode]["max_rel_err"] = float(np.max(rel))
+            res[mode]["median_rel_err"] = float(np.median(rel))
+    finally:
+        mod.free()
+    return {"workload": "spinel_10nm histograms, %d q (2theta 5-150, "
+                        "0.7107 A)" % len(K),
+            "bins": m.nbins, "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
+            "error_reference": "fp64 direct sum (device)",
+            "timing": "debye_kernel_ms: CUDA events around the contraction "
+                      "kernel (tc, tc3) or the direct-sum kernel; call_ms: "
+                      "host wall clock of dbx_intensity on resident "
+                      "histograms (prefactors, weights, reduction, D2H)",
+            "forms": {"tc": "exact 4-digit bf16 split (10 products)",
+                      "tc3": "BF16x3: 2 digits, 3 products",
+                      "fp32": "FP32 direct sum", "fp64": "FP64 direct sum"},
+            "results": res}
 
 
 def io_bench(eng, nfiles=16, seed=8):
@@ -587,6 +634,8 @@ def run_engine(args):
         line["batch256"] = batch_bench(eng, plain_models=args.plain_models)
     if not args.no_io:
         line["file_io"] = io_bench(eng)
+    if not args.no_precision:
+        line["precision"] = precision_bench(eng)
     model.free()
     eng.close()
     if not args.no_serve:
@@ -614,6 +663,8 @@ def main():
                     help="skip the serving run")
     ap.add_argument("--no-io", action="store_true",
                     help="skip the file-surface timings")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the 20,000-point precision comparison")
     ap.add_argument("--serve-seconds", type=float, default=6.0,
                     help="seconds of Poisson arrivals per rate")
     args = ap.parse_args()

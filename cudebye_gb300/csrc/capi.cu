@@ -187,7 +187,8 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
                 const dbx_species *sp, const double *K, int nq, int mode,
                 double *out_I) {
   if (nq < 1) return dbx::fail(DBX_ERR_ARG, "nq must be >= 1");
-  if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_FP64 && mode != DBX_DEBYE_FP32)
+  if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_TC3 && mode != DBX_DEBYE_FP64 &&
+      mode != DBX_DEBYE_FP32)
     return dbx::fail(DBX_ERR_ARG, "unknown Debye mode");
   bool launched = false;
   DBX_TRY(ensure_hist(c, m, rstep, nbins, &launched));
@@ -202,7 +203,7 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   DBX_TRY(dbx::debye_prefactor(sp, m->nspecies, (const double *)c->K.p, nq,
                                (double *)c->ff.p, c->stream));
   c->tm.stop(DBX_T_PREFACTOR, c->stream);
-  if (mode == DBX_DEBYE_TC) {
+  if (mode == DBX_DEBYE_TC || mode == DBX_DEBYE_TC3) {
     std::vector<dbx::TcCol> cols(np);
     for (int p = 0; p < np; ++p) {
       cols[p].hist = m->d_hist + (size_t)p * m->hist_pitch;
@@ -211,9 +212,11 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
     }
     size_t delta = 0;
     const int64_t h0 = c->tc.h2d, d0 = c->tc.d2h;
+    c->tc.classes = mode == DBX_DEBYE_TC3 ? 2 : 4;
     Error e = dbx::debye_tc(&c->tc, cols, {0, np}, rstep, K,
                             (const double *)c->K.p, nq, (double *)c->I.p,
                             c->stream, &delta, &c->tm);
+    c->tc.classes = 4;
     c->used += delta;
     c->h2d += c->tc.h2d - h0;
     c->d2h += c->tc.d2h - d0;

@@ -266,6 +266,7 @@ constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
 // Epilogue of one tile for TMEM lane `row` (0..127) of accumulator set at
 // column offset acc_col: D = acc0 + acc1 2^-8 + acc2 2^-16 + acc3 2^-24,
 // scaled, rotated by the chunk twiddle and summed over the tile's 64 chunks.
+template <int NCLS>
 __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
                                                 int mt, int nt,
                                                 const TcTile *__restrict__ tiles,
@@ -281,15 +282,19 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
   float sh = 0.f, sl = 0.f;
 #pragma unroll 1
   for (int cg = 0; cg < kTN / 16; ++cg) {
-    uint32_t a0[16], a1[16], a2[16], a3[16];
+    uint32_t a0[16], a1[16], a2[16] = {}, a3[16] = {};
     tmem_ld16(lane_base + 0 * kTN + cg * 16, a0);
     tmem_ld16(lane_base + 1 * kTN + cg * 16, a1);
-    tmem_ld16(lane_base + 2 * kTN + cg * 16, a2);
-    tmem_ld16(lane_base + 3 * kTN + cg * 16, a3);
+    if (NCLS > 2) {
+      tmem_ld16(lane_base + 2 * kTN + cg * 16, a2);
+      tmem_ld16(lane_base + 3 * kTN + cg * 16, a3);
+    }
     tmem_wait16(a0);
     tmem_wait16(a1);
-    tmem_wait16(a2);
-    tmem_wait16(a3);
+    if (NCLS > 2) {
+      tmem_wait16(a2);
+      tmem_wait16(a3);
+    }
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const int n = cg * 16 + i;
@@ -322,6 +327,10 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
   return (double)sh + (double)sl;
 }
 
+// NCLS = 4: the exact form (digit pairs with s + t <= 3). NCLS = 2: only the
+// pairs (0,0), (0,1), (1,0) — two 8-bit digits per operand and three
+// products, the BF16x3 scheme, kept for precision comparisons.
+template <int NCLS>
 __global__ void __launch_bounds__(kPThreads, 1)
     gemm_persistent_kernel(const __nv_bfloat16 *__restrict__ A,
                            const __nv_bfloat16 *__restrict__ W,
@@ -420,7 +429,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t sA = base + st * kPStageBytes, sB = sA + kASlabBytes;
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
+        for (int w = 0; w < NCLS; ++w) {
 #pragma unroll
           for (int s = 0; s <= w; ++s) {
             const int u = w - s;
@@ -465,7 +474,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
       const uint32_t lane_base =
           tmem + b * kTmemCols + ((uint32_t)((warp - 4) * 32) << 16);
       P[(size_t)nt * (2 * Qp) + mt * kTM + row] =
-          tile_epilogue(lane_base, row, mt, nt, tiles, Ecol, tw, Qp);
+          tile_epilogue<NCLS>(lane_base, row, mt, nt, tiles, Ecol, tw, Qp);
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
       if (lane == 0)
@@ -626,7 +635,10 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
                                sizeof(int) * (nmodels + 1), cudaMemcpyHostToDevice,
                                stream));
   st->h2d += sizeof(TcTile) * ntiles + sizeof(TcCol) * ncols + sizeof(int) * (nmodels + 1);
-  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel,
+  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<4>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kPSmemBytes));
+  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<2>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kPSmemBytes));
   if (!st->num_sms) {
@@ -658,8 +670,8 @@ Error tc_execute(TcState *st, const double *d_K, double *d_I,
   DBX_CUDA_TRY(cudaGetLastError());
   tm->start(DBX_T_DEBYE, stream);
   const int total = nrt * ntiles;
-  gemm_persistent_kernel<<<std::min(total, st->num_sms), kPThreads, kPSmemBytes,
-                           stream>>>(
+  auto kern = st->classes == 2 ? gemm_persistent_kernel<2> : gemm_persistent_kernel<4>;
+  kern<<<std::min(total, st->num_sms), kPThreads, kPSmemBytes, stream>>>(
       (const __nv_bfloat16 *)st->basis.p, (const __nv_bfloat16 *)st->W.p,
       (const TcTile *)st->tiles.p, (const int *)st->E.p, (const float4 *)st->twid.p,
       Qp, nrt, ntiles, (double *)st->P.p, (int *)st->err.p);

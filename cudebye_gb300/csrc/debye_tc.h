@@ -27,6 +27,9 @@ struct TcState {  // cached plan data (basis, twiddles) and workspace
   // shape of the prepared contraction
   int ncols = 0, nmodels = 0, ntiles = 0, nq = 0, Qp = 0;
   int num_sms = 0;  // persistent contraction: one CTA per SM
+  // weight classes accumulated: 4 = the exact split, 2 = the three-product
+  // (BF16x3) form used only to compare precisions
+  int classes = 4;
   double rstep = 0;
   double *S_out = nullptr;  // optional: per-column row sums S[c][q]
 };

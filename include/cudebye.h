@@ -67,6 +67,10 @@ typedef struct dbx_species {
                             pair with a global atomic (the reference's dist /
                             dist2, cuDebye-v15.cu:88-146), then the FP32
                             direct Debye sum; comparison baseline only */
+#define DBX_DEBYE_TC3 4  /* the tensor-core contraction with two 8-bit digits
+                            per operand and three products (the BF16x3
+                            scheme); not within 1e-6, for precision
+                            comparisons only (dbx_intensity, dbx_pattern) */
 
 /* ---- context ---------------------------------------------------------- */
 

@@ -122,3 +122,21 @@ def test_zero_q_matches_reference_nan(engine, orc):
     got, want = _model_case(engine, orc, m, K, "fp64")
     assert np.isnan(want[0]) and np.isnan(got[0])
     assert abs(got[1] - want[1]) <= 1e-11 * abs(want[1])
+
+
+def test_tc3_form_is_the_less_precise_study_form(engine, orc):
+    """DBX_DEBYE_TC3 (two digits, three products: BF16x3) runs through the
+    same contraction; its error is reported, not bounded by 1e-6, and it is
+    never more precise than the exact split on the same histograms."""
+    m = lattice.spinel(radius=16.0, target=4000, seed=22,
+                       grid=lattice.GRID_PRECISION)
+    tt, K = m.k_grid()
+    K = K[::8]
+    got3, want = _model_case(engine, orc, m, K, "tc3")
+    got, _ = _model_case(engine, orc, m, K, "tc")
+    rel3 = np.abs(got3 - want) / np.abs(want)
+    rel = np.abs(got - want) / np.abs(want)
+    assert np.all(np.isfinite(got3))
+    assert rel.max() <= 1e-6
+    assert rel3.max() >= rel.max()
+    assert rel3.max() < 1e-2, rel3.max()
