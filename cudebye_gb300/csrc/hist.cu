@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <thread>
 
 #include "engine.h"
 #include "hist_device.cuh"
@@ -376,6 +377,22 @@ static int64_t item_pairs(int nI, int nJ, bool diag) {
   return diag ? (int64_t)nI * (nI + 1) / 2 : (int64_t)nI * nJ;
 }
 
+// Host threads for listing tile pairs (the machine's cores, at most 32).
+static int plan_threads() {
+  static const int n = [] {
+    const unsigned h = std::thread::hardware_concurrency();
+    return (int)std::min(32u, std::max(1u, h));
+  }();
+  return n;
+}
+
+// One thread's tile pairs per window: items, their pair counts and sums.
+struct WinLists {
+  std::vector<std::vector<int2>> items;
+  std::vector<std::vector<int>> pairs;
+  std::vector<int64_t> sum;
+};
+
 void hist_plan_clear(HistPlan *plan) {
   plan->items.clear();
   plan->item_pairs.clear();
@@ -400,7 +417,6 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
   plan->window = std::max(plan->window, (int)std::min<int64_t>(W, nbins));
   const int64_t nwin = (nbins + W - 1) / W;
   const double inv = 1.0 / rstep;
-  std::vector<std::vector<int2>> per_win(nwin);
   for (size_t pi = 0; pi < pairs.size(); ++pi) {
     const int a = pairs[pi].x, b = pairs[pi].y;
     unsigned long long *row = out + (int64_t)pi * pitch;
@@ -437,27 +453,103 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       plan->nrows += 1;
       continue;
     }
-    for (auto &v : per_win) v.clear();
-    for (int I = m.tile_start[a]; I < m.tile_start[a + 1]; ++I) {
-      const int J0 = (a == b) ? I : m.tile_start[b];
-      for (int J = J0; J < m.tile_start[b + 1]; ++J) {
-        const bool diag = (a == b) && (I == J);
-        const int2 it = make_int2(I, J | (diag ? int(0x80000000u) : 0));
-        if (nwin == 1) {
-          per_win[0].push_back(it);
-          continue;
-        }
-        int64_t kmin, kmax;
-        box_bins(m.boxes[I], m.boxes[J], inv, &kmin, &kmax);
-        int64_t w0 = std::max<int64_t>(0, kmin) / W;
-        int64_t w1 = std::min<int64_t>(std::max<int64_t>(kmax, 0), nbins - 1) / W;
-        w0 = std::min(w0, nwin - 1);  // entirely beyond rmax: still run it so
-        w1 = std::max(w1, w0);        // the kernel reports the range error
-        for (int64_t w = w0; w <= w1; ++w) per_win[w].push_back(it);
+    // Tile pairs listed per window from their bounding boxes, rows of tiles
+    // split among host threads by item count; the lists are joined in row
+    // order, so the plan does not depend on the thread count.
+    const int I0 = m.tile_start[a], I1 = m.tile_start[a + 1];
+    const int Jb0 = m.tile_start[b], Jb1 = m.tile_start[b + 1];
+    auto row_items = [&](int I) -> int64_t {
+      return Jb1 - ((a == b) ? I : Jb0);
+    };
+    int64_t nitems = 0;
+    for (int I = I0; I < I1; ++I) nitems += row_items(I);
+    const int nth = (int)std::max<int64_t>(
+        1, std::min<int64_t>(plan_threads(), nitems / 4096));
+    std::vector<int> row_cut(nth + 1, I1);
+    row_cut[0] = I0;
+    {
+      int64_t acc = 0;
+      int k = 1;
+      for (int I = I0; I < I1 && k < nth; ++I) {
+        acc += row_items(I);
+        while (k < nth && acc * nth >= nitems * k) row_cut[k++] = I + 1;
       }
     }
+    std::vector<WinLists> part(nth);
+    auto list_rows = [&](int t) {
+      WinLists &L = part[t];
+      L.items.assign(nwin, {});
+      L.pairs.assign(nwin, {});
+      L.sum.assign(nwin, 0);
+      for (int I = row_cut[t]; I < row_cut[t + 1]; ++I) {
+        const int2 TI = m.tiles[I];
+        for (int J = (a == b) ? I : Jb0; J < Jb1; ++J) {
+          const bool diag = (a == b) && (I == J);
+          const int2 it = make_int2(I, J | (diag ? int(0x80000000u) : 0));
+          const int np = (int)item_pairs(TI.y, m.tiles[J].y, diag);
+          int64_t kmin, kmax;
+          box_bins(m.boxes[I], m.boxes[J], inv, &kmin, &kmax);
+          int64_t w0 = std::max<int64_t>(0, kmin) / W;
+          int64_t w1 = std::min<int64_t>(std::max<int64_t>(kmax, 0), nbins - 1) / W;
+          w0 = std::min(w0, nwin - 1);  // entirely beyond rmax: still run it
+          w1 = std::max(w1, w0);        // so the kernel reports the range error
+          for (int64_t w = w0; w <= w1; ++w) {
+            L.items[w].push_back(it);
+            L.pairs[w].push_back(np);
+            L.sum[w] += np;
+          }
+        }
+      }
+    };
+    if (nth == 1) {
+      list_rows(0);
+    } else {
+      std::vector<std::thread> th;
+      for (int t = 1; t < nth; ++t) th.emplace_back(list_rows, t);
+      list_rows(0);
+      for (std::thread &x : th) x.join();
+    }
+    // Final positions of every (window, thread) list, then one resize of
+    // the plan's arrays and a parallel copy into place.
+    std::vector<int64_t> off((size_t)nwin * nth);
+    size_t at = plan->items.size();
+    const size_t first_all = at;
+    for (int64_t w = 0; w < nwin; ++w)
+      for (int t = 0; t < nth; ++t) {
+        off[(size_t)w * nth + t] = (int64_t)at;
+        at += part[t].items[w].size();
+      }
+    if (at > plan->items.capacity()) {  // grow geometrically across calls
+      plan->items.reserve(std::max(at, 2 * plan->items.capacity()));
+      plan->item_pairs.reserve(std::max(at, 2 * plan->item_pairs.capacity()));
+    }
+    plan->items.resize(at);
+    plan->item_pairs.resize(at);
+    auto place = [&](int t) {
+      const WinLists &L = part[t];
+      for (int64_t w = 0; w < nwin; ++w) {
+        const size_t o = (size_t)off[(size_t)w * nth + t];
+        std::copy(L.items[w].begin(), L.items[w].end(), plan->items.begin() + o);
+        std::copy(L.pairs[w].begin(), L.pairs[w].end(), plan->item_pairs.begin() + o);
+      }
+    };
+    if (nth == 1) {
+      place(0);
+    } else {
+      std::vector<std::thread> th;
+      for (int t = 1; t < nth; ++t) th.emplace_back(place, t);
+      place(0);
+      for (std::thread &x : th) x.join();
+    }
+    size_t cur = first_all;
     for (int64_t w = 0; w < nwin; ++w) {
-      if (per_win[w].empty()) continue;
+      int64_t sp = 0;
+      size_t cnt = 0;
+      for (const WinLists &L : part) {
+        cnt += L.items[w].size();
+        sp += L.sum[w];
+      }
+      if (cnt == 0) continue;
       HistSeg s;
       s.atoms = m.d_atoms;
       s.tiles = m.d_tiles;
@@ -468,17 +560,10 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       s.nbins = (unsigned)nbins;
       s.shape = kSegList;
       s.ti0 = s.tni = s.tj0 = s.tnj = 0;
-      const int first = (int)plan->items.size();
-      int64_t sp = 0;
-      for (const int2 &it : per_win[w]) {
-        const int2 TI = m.tiles[it.x], TJ = m.tiles[it.y & 0x7fffffff];
-        plan->items.push_back(it);
-        plan->item_pairs.push_back((int)item_pairs(TI.y, TJ.y, it.y < 0));
-        sp += plan->item_pairs.back();
-      }
       plan->segs.push_back(s);
-      plan->seg_items.push_back(make_int2(first, (int)plan->items.size()));
+      plan->seg_items.push_back(make_int2((int)cur, (int)(cur + cnt)));
       plan->seg_pairs.push_back(sp);
+      cur += cnt;
     }
     plan->pairs += block_pairs;
     plan->nrows += 1;

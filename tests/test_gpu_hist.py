@@ -53,6 +53,18 @@ def test_multi_window(engine, orc):
     gpu_vs_oracle(engine, orc, m.xyz, m.counts, 1e-4, nbins)
 
 
+@pytest.mark.parametrize("rstep", [4e-4, 1.5e-4, 4e-5])
+def test_fine_bins_many_windows(engine, orc, rstep):
+    """A 25,000-atom spinel-like particle binned finer than one window
+    holds: 155,002 bins (2 windows), 413,335 (4) and 1,550,001 (14); tile
+    pairs are listed per window from their bounding boxes, and every bin
+    equals the oracle's."""
+    m = lattice.spinel(radius=30.0, target=25000, seed=13, rstep=rstep)
+    nbins = cd.channels(m.rmax, rstep)
+    h = gpu_vs_oracle(engine, orc, m.xyz, m.counts, rstep, nbins)
+    assert int(h.sum()) == m.pairs
+
+
 def test_single_pair_entry_point(engine, orc):
     m = lattice.spinel(radius=12.0, target=1200, seed=12)
     mod = engine.upload(m.xyz, m.counts)
