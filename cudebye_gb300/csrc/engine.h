@@ -138,7 +138,7 @@ constexpr int kSegList = 0, kSegRect = 1, kSegTri = 2;
 struct HistTask {  // one CTA-sized slice of a segment's tile pairs
   int seg;
   int item_begin, item_end;
-  int pad;
+  int next;  // the task that the k-th pull of the task counter runs (entry k)
 };
 struct HistRow {  // an output histogram to zero before a launch
   unsigned long long *out;

@@ -157,8 +157,10 @@ __device__ __forceinline__ int2 seg_item(const HistSeg &sg,
                    (sg.ti0 + j) | (i == j ? int(0x80000000u) : 0));
 }
 
-// One warp = one tile pair (128 x 128 atoms). CTAs pull equal-sized tasks
-// from a global counter; task t's packed window goes to partial slot t.
+// One warp = one tile pair (128 x 128 atoms). CTAs pull tasks from a global
+// counter in the order tasks[k].next (decreasing size, so the last tasks
+// to start are the short ones); task t's packed window goes to partial
+// slot t.
 __global__ void __launch_bounds__(kHistThreads, 1)
     hist_tiles_kernel(const int2 *__restrict__ items,
                       const HistTask *__restrict__ tasks, int ntasks,
@@ -170,7 +172,10 @@ __global__ void __launch_bounds__(kHistThreads, 1)
   __shared__ int s_task;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (;;) {
-    if (threadIdx.x == 0) s_task = atomicAdd(task_counter, 1);
+    if (threadIdx.x == 0) {  // tasks are pulled largest first
+      const int k = atomicAdd(task_counter, 1);
+      s_task = k < ntasks ? tasks[k].next : ntasks;
+    }
     __syncthreads();
     const int t = s_task;
     if (t >= ntasks) break;
@@ -609,6 +614,26 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
     }
     sg.task_end = (int)plan->tasks.size();
   }
+  // Pull order: decreasing binned pairs (longest task first), ties in task
+  // order. Implicit segments' tasks are costed by their share of items.
+  std::vector<double> cost(plan->tasks.size());
+  for (size_t t = 0; t < plan->tasks.size(); ++t) {
+    const HistTask &tk = plan->tasks[t];
+    const int2 si = plan->seg_items[tk.seg];
+    if (plan->segs[tk.seg].shape != kSegList) {
+      cost[t] = (double)plan->seg_pairs[tk.seg] * (tk.item_end - tk.item_begin) /
+                std::max(1, si.y - si.x);
+    } else {
+      double c = 0;
+      for (int i = tk.item_begin; i < tk.item_end; ++i) c += plan->item_pairs[i];
+      cost[t] = c;
+    }
+  }
+  std::vector<int> order(plan->tasks.size());
+  for (size_t t = 0; t < order.size(); ++t) order[t] = (int)t;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return cost[x] > cost[y]; });
+  for (size_t k = 0; k < order.size(); ++k) plan->tasks[k].next = order[k];
 }
 
 Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
