@@ -409,7 +409,8 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
   }
   // species may change between passes (re-scoring): upload every pass
   Error e = dbx::prefactor_upload(&b.pref, sp, nsp, b.col_sp.data(),
-                                  (int)b.col_sp.size(), c->stream, &delta);
+                                  (int)b.col_sp.size(), (int)b.K.size(),
+                                  c->stream, &delta);
   c->used += delta;
   c->h2d += sizeof(dbx_species) * nsp + sizeof(int2) * b.col_sp.size();
   if (e.code) return e;
@@ -418,7 +419,8 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
       c->hws.partial.p,   c->hws.oor.p,      b.pref.sp.p,        b.pref.colsp.p,
       b.ff.p,             b.I.p,             b.K_dev.p,          c->tc.W.p,
       c->tc.E.p,          c->tc.P.p,         c->tc.tiles.p,      c->tc.cols.p,
-      c->tc.basis.p,      c->tc.twid.p,      c->tc.nonself.p,    c->tc.err.p};
+      c->tc.basis.p,      c->tc.twid.p,      c->tc.nonself.p,    c->tc.err.p,
+      b.pref.f.p,         b.pref.fid.p};
   if (c->graphs) {
     if (!b.exec || b.graph_ptrs != ptrs) {
       drop_graph(&b);
@@ -558,7 +560,8 @@ int dbx_destroy(dbx_ctx *c) {
   if (c->batch.graph) cudaGraphDestroy(c->batch.graph);
   for (dbx::DevBuf *b : {&c->batch.hp.lists.items, &c->batch.hp.lists.segs,
                          &c->batch.hp.lists.tasks, &c->batch.hp.lists.rows,
-                         &c->batch.pref.sp, &c->batch.pref.colsp, &c->batch.ff,
+                         &c->batch.pref.sp, &c->batch.pref.colsp,
+                         &c->batch.pref.f, &c->batch.pref.fid, &c->batch.ff,
                          &c->batch.I, &c->batch.K_dev})
     release(c, b);
   dbx::tc_release(&c->tc);

@@ -1,7 +1,8 @@
 // debye.cu — Debye sum kernels on sm_103a (hot path 2, direct forms).
 //
-//  * debye_prefactor_kernel: the reference's atomicScatter
-//    (cuDebye-v15.cu:447-467), one thread per (pair, q), FP64.
+//  * species_f_kernel + debye_prefactor_kernel / prefactor_cols_kernel: the
+//    reference's atomicScatter (cuDebye-v15.cu:447-467) in FP64, the form
+//    factor once per (species, q), the pair product once per (pair, q).
 //  * debye_direct_kernel<T>: the reference's debyeRowSum arithmetic
 //    (cuDebye-v15.cu:493-538) for all pairs of a model at once: one thread
 //    per q, bins staged through shared memory, sinc evaluated once per
@@ -12,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "engine.h"
@@ -22,9 +24,45 @@ struct SpeciesDev {
   double occ, beq, a[5], b[5], c;
 };
 
+// f_s(q) = c + sum_i a_i exp(b_i nhs), nhs = -K^2/(16 pi^2): the form
+// factor of atomicScatter (cuDebye-v15.cu:452-462), computed once per q and
+// distinct coefficient set; the pair kernels read it instead of recomputing
+// both factors for every pair (same operations, same values). Row u is
+// species rep[u] (rep null: species u); rows with rep[u] < 0 are unused.
+__global__ void species_f_kernel(const SpeciesDev *__restrict__ sp,
+                                 const int *__restrict__ rep,
+                                 const double *__restrict__ K, int nq,
+                                 double *__restrict__ F) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int u = blockIdx.y;
+  const int s = rep ? rep[u] : u;
+  if (q >= nq || s < 0) return;
+  const SpeciesDev &sd = sp[s];
+  const double rp16pi2 = -0.006332573977646;  // cuDebye-v15.cu:452
+  const double nhs = K[q] * K[q] * rp16pi2;
+  double f = sd.c;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) f += sd.a[i] * exp(sd.b[i] * nhs);
+  F[(size_t)u * nq + q] = f;
+}
+
+// ff = (o1 o2) exp(nhs (B1 + B2)) f1 f2 in the reference's order
+// (cuDebye-v15.cu:463-465).
+__device__ __forceinline__ double pair_prefactor(const SpeciesDev &s1,
+                                                 const SpeciesDev &s2,
+                                                 double Kq, double f1,
+                                                 double f2) {
+  const double rp16pi2 = -0.006332573977646;  // cuDebye-v15.cu:452
+  const double nhs = Kq * Kq * rp16pi2;
+  double v = s1.occ * s2.occ;
+  v = v * exp(nhs * (s1.beq + s2.beq));
+  return v * f1 * f2;
+}
+
 __global__ void debye_prefactor_kernel(const SpeciesDev *__restrict__ sp,
                                        int nspecies,
                                        const double *__restrict__ K, int nq,
+                                       const double *__restrict__ F,
                                        double *__restrict__ ff) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int p = blockIdx.y;
@@ -36,32 +74,32 @@ __global__ void debye_prefactor_kernel(const SpeciesDev *__restrict__ sp,
     ++row;
   }
   const int col = row + rem;
-  const SpeciesDev &s1 = sp[row], &s2 = sp[col];
-  const double rp16pi2 = -0.006332573977646;  // cuDebye-v15.cu:452
-  const double nhs = K[q] * K[q] * rp16pi2;
-  double v = s1.occ * s2.occ;
-  v = v * exp(nhs * (s1.beq + s2.beq));
-  double f1 = s1.c, f2 = s2.c;
-#pragma unroll
-  for (int i = 0; i < 5; ++i) {
-    f1 += s1.a[i] * exp(s1.b[i] * nhs);
-    f2 += s2.a[i] * exp(s2.b[i] * nhs);
-  }
-  ff[(size_t)p * nq + q] = v * f1 * f2;
+  ff[(size_t)p * nq + q] = pair_prefactor(sp[row], sp[col], K[q],
+                                          F[(size_t)row * nq + q],
+                                          F[(size_t)col * nq + q]);
 }
 
 Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
                       int nq, double *d_ff, cudaStream_t stream) {
   static_assert(sizeof(SpeciesDev) == sizeof(dbx_species), "layout");
   SpeciesDev *d_sp = nullptr;
+  double *d_F = nullptr;
   DBX_CUDA_TRY(cudaMallocAsync((void **)&d_sp, sizeof(SpeciesDev) * nspecies,
                                stream));
-  DBX_CUDA_TRY(cudaMemcpyAsync(d_sp, sp, sizeof(SpeciesDev) * nspecies,
-                               cudaMemcpyHostToDevice, stream));
-  dim3 grid((nq + 127) / 128, npairs_of(nspecies));
-  debye_prefactor_kernel<<<grid, 128, 0, stream>>>(d_sp, nspecies, d_K, nq,
-                                                   d_ff);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = cudaMallocAsync((void **)&d_F,
+                                  sizeof(double) * nq * (size_t)nspecies, stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_sp, sp, sizeof(SpeciesDev) * nspecies,
+                        cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) {
+    species_f_kernel<<<dim3((nq + 127) / 128, nspecies), 128, 0, stream>>>(
+        d_sp, nullptr, d_K, nq, d_F);
+    dim3 grid((nq + 127) / 128, npairs_of(nspecies));
+    debye_prefactor_kernel<<<grid, 128, 0, stream>>>(d_sp, nspecies, d_K, nq,
+                                                     d_F, d_ff);
+    e = cudaGetLastError();
+  }
+  if (d_F) cudaFreeAsync(d_F, stream);
   cudaFreeAsync(d_sp, stream);
   if (e != cudaSuccess)
     return fail(DBX_ERR_CUDA, std::string("prefactor: ") + cudaGetErrorString(e));
@@ -69,26 +107,21 @@ Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
 }
 
 // Prefactor of many (model, pair) columns at once: column c uses species
-// col_sp[c] = {a, b} of the concatenated species array.
+// col_sp[c] = {a, b} of the concatenated species array, whose form factors
+// are rows fid[a], fid[b] of F.
 __global__ void prefactor_cols_kernel(const SpeciesDev *__restrict__ sp,
                                       const int2 *__restrict__ col_sp,
+                                      const int *__restrict__ fid,
                                       const double *__restrict__ K, int nq,
+                                      const double *__restrict__ F,
                                       double *__restrict__ ff) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (q >= nq) return;
-  const SpeciesDev &s1 = sp[col_sp[c].x], &s2 = sp[col_sp[c].y];
-  const double rp16pi2 = -0.006332573977646;  // cuDebye-v15.cu:452
-  const double nhs = K[q] * K[q] * rp16pi2;
-  double v = s1.occ * s2.occ;
-  v = v * exp(nhs * (s1.beq + s2.beq));
-  double f1 = s1.c, f2 = s2.c;
-#pragma unroll
-  for (int i = 0; i < 5; ++i) {
-    f1 += s1.a[i] * exp(s1.b[i] * nhs);
-    f2 += s2.a[i] * exp(s2.b[i] * nhs);
-  }
-  ff[(size_t)c * nq + q] = v * f1 * f2;
+  const int2 ab = col_sp[c];
+  ff[(size_t)c * nq + q] = pair_prefactor(sp[ab.x], sp[ab.y], K[q],
+                                          F[(size_t)fid[ab.x] * nq + q],
+                                          F[(size_t)fid[ab.y] * nq + q]);
 }
 
 static Error grow_buf(DevBuf *b, size_t bytes, size_t *delta) {
@@ -106,23 +139,54 @@ static Error grow_buf(DevBuf *b, size_t bytes, size_t *delta) {
 }
 
 Error prefactor_upload(PrefState *st, const dbx_species *sp, int nsp,
-                       const int2 *col_sp, int ncols, cudaStream_t stream,
-                       size_t *delta) {
+                       const int2 *col_sp, int ncols, int nq,
+                       cudaStream_t stream, size_t *delta) {
   DBX_TRY(grow_buf(&st->sp, sizeof(SpeciesDev) * std::max(nsp, 1), delta));
   DBX_TRY(grow_buf(&st->colsp, sizeof(int2) * std::max(ncols, 1), delta));
+  DBX_TRY(grow_buf(&st->f, sizeof(double) * std::max(nsp, 1) * (size_t)std::max(nq, 1),
+                   delta));
   DBX_CUDA_TRY(cudaMemcpyAsync(st->sp.p, sp, sizeof(SpeciesDev) * nsp,
                                cudaMemcpyHostToDevice, stream));
   DBX_CUDA_TRY(cudaMemcpyAsync(st->colsp.p, col_sp, sizeof(int2) * ncols,
                                cudaMemcpyHostToDevice, stream));
+  // species with equal form-factor coefficients (a, b, c) share one row of
+  // F: a batch of many models holds few distinct elements
+  std::vector<int> ids(2 * (size_t)std::max(nsp, 1), -1);  // fid, then rep
+  int nu = 0;
+  for (int i = 0; i < nsp; ++i) {
+    int u = 0;
+    for (; u < nu; ++u) {
+      const dbx_species &r = sp[ids[nsp + u]];
+      if (std::memcmp(r.a, sp[i].a, sizeof r.a) == 0 &&
+          std::memcmp(r.b, sp[i].b, sizeof r.b) == 0 &&
+          std::memcmp(&r.c, &sp[i].c, sizeof r.c) == 0)
+        break;
+    }
+    if (u == nu) ids[nsp + nu++] = i;
+    ids[i] = u;
+  }
+  DBX_TRY(grow_buf(&st->fid, sizeof(int) * ids.size(), delta));
+  DBX_CUDA_TRY(cudaMemcpyAsync(st->fid.p, ids.data(), sizeof(int) * ids.size(),
+                               cudaMemcpyHostToDevice, stream));
   st->ncols = ncols;
+  st->nsp = nsp;
   return ok();
 }
 
 Error prefactor_execute(const PrefState &st, const double *d_K, int nq,
                         double *d_ff, cudaStream_t stream) {
+  if (st.f.bytes < sizeof(double) * std::max(st.nsp, 1) * (size_t)nq)
+    return fail(DBX_ERR_ARG, "prefactor: q grid larger than prepared");
+  // one block row per species; rows past the distinct sets return at once
+  // (the launch shape does not depend on the coefficients, so a captured
+  // graph stays valid when a re-score changes them)
+  const int *fid = (const int *)st.fid.p;
+  species_f_kernel<<<dim3((nq + 127) / 128, st.nsp), 128, 0, stream>>>(
+      (const SpeciesDev *)st.sp.p, fid + st.nsp, d_K, nq, (double *)st.f.p);
   dim3 grid((nq + 127) / 128, st.ncols);
   prefactor_cols_kernel<<<grid, 128, 0, stream>>>(
-      (const SpeciesDev *)st.sp.p, (const int2 *)st.colsp.p, d_K, nq, d_ff);
+      (const SpeciesDev *)st.sp.p, (const int2 *)st.colsp.p, fid, d_K, nq,
+      (const double *)st.f.p, d_ff);
   DBX_CUDA_TRY(cudaGetLastError());
   return ok();
 }

@@ -5,7 +5,8 @@
 //     S(q) = sum_k m_k sin(q r_k)/(q r_k),   r_k = k*rstep,
 // with m_k = 2 n_k off the self distance (r_k > 0.0005) and n_k on it.
 // Here the non-self part is rewritten as q*S'(q) = sum_k w_k sin(q r_k) with
-// w_k = m_k / r_k, and the bins are cut into chunks of L = 256:
+// w_k = m_k / r_k = (2 / rstep) n_k / k, and the bins are cut into chunks of
+// L = 256:
 // k = k0 + j, k0 = ch*L, so sin(q r_k) = sin(q k0 dr) cos(q j dr)
 //                                       + cos(q k0 dr) sin(q j dr).
 // The j-basis [cos(q j dr) | sin(q j dr)] is the same for every chunk, so
@@ -126,11 +127,17 @@ __global__ void twiddle_kernel(const double *__restrict__ K, int nq, int Qp,
   tw[idx] = make_float4(sh, (float)(s - (double)sh), ch_, (float)(c - (double)ch_));
 }
 
-// Chunk weights w = m/r as digits, one warp per (tile, column).
+// Chunk weights as digits, one warp per (tile, column). The weight of bin
+// k is w_k = m_k / r_k = (2 / rstep) (n_k / k) off the self distance
+// (k >= kself, the first bin with k rstep > 0.0005); the common factor
+// 2 / rstep is applied to the column sums (reduce_kernel), so the digits
+// hold u_k = n_k / k, computed in integers: fixed31(u_k 2^-e) =
+// round(n_k 2^(31-e) / k), with e the chunk's scale exponent (every
+// u_k < 2^e). No FP64 arithmetic (slow on this part) is needed.
 // Layout of W: [col tile][slab][digit][tiled 64 x 64]; E: per column,
-// the chunk's scale exponent (max|w| < 2^E).
+// the chunk's scale exponent.
 __global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
-                               const TcCol *__restrict__ cols, double rstep,
+                               const TcCol *__restrict__ cols, long long kself,
                                __nv_bfloat16 *__restrict__ W,
                                int *__restrict__ E,
                                int *__restrict__ nonself) {
@@ -141,32 +148,50 @@ __global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
   const TcTile t = tiles[nt];
   const TcCol col = cols[t.col];
   const int ch = t.ch0 + n;
-  double w[8];
-  double mx = 0.0;
+  unsigned long long cnt[8];
+  float mx = 0.f;
+  bool any = false;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const long long k = (long long)ch * kL + lane * 8 + i;
-    double v = 0.0;
-    if (k < col.nbins) {
-      const double cnt = (double)col.hist[k];
-      const double r = (double)k * rstep;  // r_reduced (cuDebye-v15.cu:735)
-      if (r > kSelfR && cnt != 0.0) v = (2.0 * cnt) / r;
-    }
-    w[i] = v;
-    mx = fmax(mx, fabs(v));
+    unsigned long long c = 0;
+    if (k < col.nbins && k >= kself && k > 0) c = col.hist[k];
+    cnt[i] = c;
+    any |= c != 0;
+    if (c) mx = fmaxf(mx, (float)c / (float)k);  // estimate of u_k
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  any = __any_sync(0xffffffffu, any);
   int e = 0;
-  if (mx > 0.0) frexp(mx, &e);  // mx < 2^e
-  const double scale = ldexp(1.0, -e);  // |w * scale| < 1; fixed31 adds 2^31
+  if (any) {
+    frexpf(mx, &e);  // mx < 2^e; exact check below, u_k < 2^e
+    bool over = false;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const unsigned long long k = (unsigned long long)ch * kL + lane * 8 + i;
+      // n >= k 2^e, exactly: floor(n / 2^e) >= k, or n 2^-e >= k for e < 0
+      // (then n < k < 2^22, no overflow)
+      if (cnt[i] && e < 64) over |= e >= 0 ? (cnt[i] >> e) >= k : (cnt[i] << -e) >= k;
+    }
+    if (__any_sync(0xffffffffu, over)) ++e;
+  }
   const int j0 = lane * 8, ks = j0 / kKS, k0 = j0 % kKS;
   const size_t base = (size_t)(nt * kNSlab + ks) * kND * kBBlock + tiled_off(n, k0);
   alignas(16) __nv_bfloat16 dig[kND][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
+    long long f = 0;
+    if (cnt[i]) {
+      const unsigned long long k = (unsigned long long)ch * kL + lane * 8 + i;
+      // n 2^(31-e) / k rounded; n < k 2^e keeps every operand below 2^53
+      const unsigned long long num = e <= 31 ? cnt[i] << (31 - e) : cnt[i];
+      const unsigned long long den = e <= 31 ? k : k << (e - 31);
+      f = (long long)((num + den / 2) / den);
+      f = f > 2147483647LL ? 2147483647LL : f;
+    }
     float d[4];
-    split4(fixed31(w[i] * scale), d);
+    split4(f, d);
 #pragma unroll
     for (int s = 0; s < kND; ++s) dig[s][i] = __float2bfloat16_rn(d[s]);
   }
@@ -176,7 +201,7 @@ __global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
         *reinterpret_cast<const uint4 *>(dig[s]);
   if (lane == 0) {
     E[nt * kTN + n] = e;
-    if (mx > 0.0) atomicOr(&nonself[t.col], 1);
+    if (any) atomicOr(&nonself[t.col], 1);
   }
 }
 
@@ -491,13 +516,14 @@ __global__ void __launch_bounds__(kPThreads, 1)
 }
 
 // I[model][q] = sum over the model's columns (pair order) of
-// ff[q] * (self + (sum of the column's tiles of P over both row halves)/K).
+// ff[q] * (self + (2 / rstep) (sum of the column's tiles of P over both
+// row halves) / K).
 __global__ void reduce_kernel(const TcCol *__restrict__ cols, int ncols,
                               const int *__restrict__ model_col_begin,
                               int nmodels, const double *__restrict__ P,
                               const int *__restrict__ nonself,
                               const double *__restrict__ K, int nq, int Qp,
-                              double *__restrict__ I,
+                              double wscale, double *__restrict__ I,
                               double *__restrict__ S_out) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int mod = blockIdx.y;
@@ -513,7 +539,7 @@ __global__ void reduce_kernel(const TcCol *__restrict__ cols, int ncols,
     if (Kq == 0.0)  // sin(0)/0 of the reference (cuDebye-v15.cu:509)
       S = nonself[c] ? __longlong_as_double(0x7ff8000000000000LL) : col.self;
     else
-      S = col.self + t / Kq;
+      S = col.self + (t * wscale) / Kq;  // wscale = 2 / rstep
     if (S_out) S_out[(size_t)c * nq + q] = S;
     acc += S * col.ff[q];
   }
@@ -664,8 +690,10 @@ Error tc_execute(TcState *st, const double *d_K, double *d_I,
   self_kernel<<<(ncols + 127) / 128, 128, 0, stream>>>((TcCol *)st->cols.p, ncols,
                                                        st->rstep);
   const long long nwarps = (long long)ntiles * kTN;
+  long long kself = 0;  // first bin beyond the self distance
+  while ((double)kself * st->rstep <= kSelfR) ++kself;
   weights_kernel<<<(unsigned)((nwarps * 32 + 255) / 256), 256, 0, stream>>>(
-      (const TcTile *)st->tiles.p, ntiles, (const TcCol *)st->cols.p, st->rstep,
+      (const TcTile *)st->tiles.p, ntiles, (const TcCol *)st->cols.p, kself,
       (__nv_bfloat16 *)st->W.p, (int *)st->E.p, (int *)st->nonself.p);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->start(DBX_T_DEBYE, stream);
@@ -680,8 +708,8 @@ Error tc_execute(TcState *st, const double *d_K, double *d_I,
   dim3 rg((nq + 127) / 128, st->nmodels);
   reduce_kernel<<<rg, 128, 0, stream>>>(
       (const TcCol *)st->cols.p, ncols, (const int *)st->mcb.p, st->nmodels,
-      (const double *)st->P.p, (const int *)st->nonself.p, d_K, nq, Qp, d_I,
-      st->S_out);
+      (const double *)st->P.p, (const int *)st->nonself.p, d_K, nq, Qp,
+      2.0 / st->rstep, d_I, st->S_out);
   DBX_CUDA_TRY(cudaGetLastError());
   return ok();
 }

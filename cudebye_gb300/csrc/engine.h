@@ -224,13 +224,15 @@ Error check_sqrt(unsigned lo, unsigned hi, int num_sms, cudaStream_t stream,
 
 // ---- Debye kernels (debye.cu) ----------------------------------------------
 struct PrefState {  // species and column descriptors of a batched prefactor
-  DevBuf sp, colsp;
-  int ncols = 0;
+  DevBuf sp, colsp, f, fid;  // f: form factors [distinct set][q]; fid:
+                             // species -> row of f, then row -> species
+  int ncols = 0, nsp = 0;
 };
-// Upload species (concatenated) and per-column species pairs {a, b}.
+// Upload species (concatenated) and per-column species pairs {a, b}; room
+// for the form factors of nq q values.
 Error prefactor_upload(PrefState *st, const dbx_species *sp, int nsp,
-                       const int2 *col_sp, int ncols, cudaStream_t stream,
-                       size_t *bytes_delta);
+                       const int2 *col_sp, int ncols, int nq,
+                       cudaStream_t stream, size_t *bytes_delta);
 // ff[c][q] for every column (kernel only; capturable).
 Error prefactor_execute(const PrefState &st, const double *d_K, int nq,
                         double *d_ff, cudaStream_t stream);

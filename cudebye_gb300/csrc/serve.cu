@@ -127,7 +127,8 @@ size_t lane_need(const Req &r, int nspecies) {
   const size_t np = npairs_of(nspecies);
   const size_t nch = (size_t)(r.nbins + 255) / 256, tiles = np * ((nch + 63) / 64);
   return tiles * 128 * 1024 + tiles * 2 * Qp * 8 + (2 * Qp / 128) * 256 * 1024 +
-         ((nch + 63) / 64 * 64) * Qp * 16 + np * nq * 8 * 2 + nq * 8;
+         ((nch + 63) / 64 * 64) * Qp * 16 + np * nq * 8 * 2 + nq * 8 +
+         (size_t)nspecies * nq * 8;
 }
 
 }  // namespace
@@ -338,8 +339,8 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
     std::vector<int2> col_sp;
     for (int a = 0; a < P; ++a)
       for (int b = a; b < P; ++b) col_sp.push_back(make_int2(a, b));
-    DBX_TRY(prefactor_upload(&L.pref, r->sp.data(), P, col_sp.data(), np, st,
-                             &used_delta));
+    DBX_TRY(prefactor_upload(&L.pref, r->sp.data(), P, col_sp.data(), np, nq,
+                             st, &used_delta));
     DBX_TRY(prefactor_execute(L.pref, (const double *)L.K.p, nq, (double *)L.ff.p, st));
     double *dI = (double *)L.I.p + r->offset;
     if (r->kind == kSameGrid) {
@@ -608,7 +609,7 @@ int dbx_server_destroy(dbx_server *s) {
   }
   for (dbx::Lane &L : s->lanes) {
     for (dbx::DevBuf *b : {&L.hws.items, &L.hws.segs, &L.hws.tasks, &L.hws.rows,
-                           &L.hws.partial, &L.hws.oor, &L.pref.sp, &L.pref.colsp,
+                           &L.hws.partial, &L.hws.oor, &L.pref.sp, &L.pref.colsp, &L.pref.f, &L.pref.fid,
                            &L.K, &L.ff, &L.I})
       dbx::release(b);
     dbx::tc_release(&L.tc);
