@@ -124,31 +124,16 @@ __global__ void prefactor_cols_kernel(const SpeciesDev *__restrict__ sp,
                                           F[(size_t)fid[ab.y] * nq + q]);
 }
 
-static Error grow_buf(DevBuf *b, size_t bytes, size_t *delta) {
-  if (b->bytes >= bytes) return ok();
-  if (b->p) {
-    cudaFree(b->p);
-    *delta -= b->bytes;
-    b->p = nullptr;
-    b->bytes = 0;
-  }
-  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
-  b->bytes = bytes;
-  *delta += bytes;
-  return ok();
-}
-
 Error prefactor_upload(PrefState *st, const dbx_species *sp, int nsp,
                        const int2 *col_sp, int ncols, int nq,
                        cudaStream_t stream, size_t *delta) {
-  DBX_TRY(grow_buf(&st->sp, sizeof(SpeciesDev) * std::max(nsp, 1), delta));
-  DBX_TRY(grow_buf(&st->colsp, sizeof(int2) * std::max(ncols, 1), delta));
-  DBX_TRY(grow_buf(&st->f, sizeof(double) * std::max(nsp, 1) * (size_t)std::max(nq, 1),
-                   delta));
-  DBX_CUDA_TRY(cudaMemcpyAsync(st->sp.p, sp, sizeof(SpeciesDev) * nsp,
-                               cudaMemcpyHostToDevice, stream));
-  DBX_CUDA_TRY(cudaMemcpyAsync(st->colsp.p, col_sp, sizeof(int2) * ncols,
-                               cudaMemcpyHostToDevice, stream));
+  const cudaStream_t as = st->alloc_stream;
+  DBX_TRY(buf_grow(&st->sp, sizeof(SpeciesDev) * std::max(nsp, 1), delta, as));
+  DBX_TRY(buf_grow(&st->colsp, sizeof(int2) * std::max(ncols, 1), delta, as));
+  DBX_TRY(buf_grow(&st->f, sizeof(double) * std::max(nsp, 1) * (size_t)std::max(nq, 1),
+                   delta, as));
+  DBX_TRY(h2d_copy(st->sp.p, sp, sizeof(SpeciesDev) * nsp, stream, st->arena));
+  DBX_TRY(h2d_copy(st->colsp.p, col_sp, sizeof(int2) * ncols, stream, st->arena));
   // species with equal form-factor coefficients (a, b, c) share one row of
   // F: a batch of many models holds few distinct elements
   std::vector<int> ids(2 * (size_t)std::max(nsp, 1), -1);  // fid, then rep
@@ -165,9 +150,8 @@ Error prefactor_upload(PrefState *st, const dbx_species *sp, int nsp,
     if (u == nu) ids[nsp + nu++] = i;
     ids[i] = u;
   }
-  DBX_TRY(grow_buf(&st->fid, sizeof(int) * ids.size(), delta));
-  DBX_CUDA_TRY(cudaMemcpyAsync(st->fid.p, ids.data(), sizeof(int) * ids.size(),
-                               cudaMemcpyHostToDevice, stream));
+  DBX_TRY(buf_grow(&st->fid, sizeof(int) * ids.size(), delta, as));
+  DBX_TRY(h2d_copy(st->fid.p, ids.data(), sizeof(int) * ids.size(), stream, st->arena));
   st->ncols = ncols;
   st->nsp = nsp;
   return ok();

@@ -573,20 +573,6 @@ __global__ void self_kernel(TcCol *cols, int ncols, double rstep) {
 
 using namespace tc;
 
-static Error grow(DevBuf *b, size_t bytes, size_t *delta) {
-  if (b->bytes >= bytes) return ok();
-  if (b->p) {
-    cudaFree(b->p);
-    *delta -= b->bytes;
-    b->p = nullptr;
-    b->bytes = 0;
-  }
-  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
-  b->bytes = bytes;
-  *delta += bytes;
-  return ok();
-}
-
 void tc_release(TcState *st) {
   for (DevBuf *b : {&st->basis, &st->twid, &st->W, &st->E, &st->P, &st->tiles,
                     &st->cols, &st->mcb, &st->nonself, &st->err})
@@ -628,20 +614,21 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
   const int nch_cap = (nch_max + kTN - 1) / kTN * kTN;  // twiddle rows
   const int ntiles = (int)tiles.size();
   // Plan data cached per (q grid, rstep, chunk count): basis and twiddles.
+  const cudaStream_t as = st->alloc_stream;
   const bool same_grid = st->grid_K.size() == (size_t)nq && st->grid_rstep == rstep &&
                          st->grid_nch >= nch_cap &&
                          std::memcmp(st->grid_K.data(), h_K, sizeof(double) * nq) == 0;
-  DBX_TRY(grow(&st->W, (size_t)ntiles * kNSlab * kBSlabBytes, delta));
-  DBX_TRY(grow(&st->E, sizeof(int) * ntiles * kTN, delta));
-  DBX_TRY(grow(&st->P, sizeof(double) * ntiles * 2 * Qp, delta));
-  DBX_TRY(grow(&st->tiles, sizeof(TcTile) * ntiles, delta));
-  DBX_TRY(grow(&st->cols, sizeof(TcCol) * ncols, delta));
-  DBX_TRY(grow(&st->mcb, sizeof(int) * (nmodels + 1), delta));
-  DBX_TRY(grow(&st->nonself, sizeof(int) * ncols, delta));
-  DBX_TRY(grow(&st->err, sizeof(int), delta));
+  DBX_TRY(buf_grow(&st->W, (size_t)ntiles * kNSlab * kBSlabBytes, delta, as));
+  DBX_TRY(buf_grow(&st->E, sizeof(int) * ntiles * kTN, delta, as));
+  DBX_TRY(buf_grow(&st->P, sizeof(double) * ntiles * 2 * Qp, delta, as));
+  DBX_TRY(buf_grow(&st->tiles, sizeof(TcTile) * ntiles, delta, as));
+  DBX_TRY(buf_grow(&st->cols, sizeof(TcCol) * ncols, delta, as));
+  DBX_TRY(buf_grow(&st->mcb, sizeof(int) * (nmodels + 1), delta, as));
+  DBX_TRY(buf_grow(&st->nonself, sizeof(int) * ncols, delta, as));
+  DBX_TRY(buf_grow(&st->err, sizeof(int), delta, as));
   if (!same_grid) {
-    DBX_TRY(grow(&st->basis, (size_t)nrt * kNSlab * kASlabBytes, delta));
-    DBX_TRY(grow(&st->twid, sizeof(float4) * (size_t)nch_cap * Qp, delta));
+    DBX_TRY(buf_grow(&st->basis, (size_t)nrt * kNSlab * kASlabBytes, delta, as));
+    DBX_TRY(buf_grow(&st->twid, sizeof(float4) * (size_t)nch_cap * Qp, delta, as));
     const long long nb = 2LL * Qp * kL;
     basis_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, stream>>>(
         d_K, nq, Qp, rstep, (__nv_bfloat16 *)st->basis.p);
@@ -653,21 +640,19 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
     st->grid_rstep = rstep;
     st->grid_nch = nch_cap;
   }
-  DBX_CUDA_TRY(cudaMemcpyAsync(st->tiles.p, tiles.data(), sizeof(TcTile) * ntiles,
-                               cudaMemcpyHostToDevice, stream));
-  DBX_CUDA_TRY(cudaMemcpyAsync(st->cols.p, cols.data(), sizeof(TcCol) * ncols,
-                               cudaMemcpyHostToDevice, stream));
-  DBX_CUDA_TRY(cudaMemcpyAsync(st->mcb.p, model_col_begin.data(),
-                               sizeof(int) * (nmodels + 1), cudaMemcpyHostToDevice,
-                               stream));
+  DBX_TRY(h2d_copy(st->tiles.p, tiles.data(), sizeof(TcTile) * ntiles, stream,
+                   st->arena));
+  DBX_TRY(h2d_copy(st->cols.p, cols.data(), sizeof(TcCol) * ncols, stream, st->arena));
+  DBX_TRY(h2d_copy(st->mcb.p, model_col_begin.data(), sizeof(int) * (nmodels + 1),
+                   stream, st->arena));
   st->h2d += sizeof(TcTile) * ntiles + sizeof(TcCol) * ncols + sizeof(int) * (nmodels + 1);
-  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<4>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kPSmemBytes));
-  DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<2>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kPSmemBytes));
-  if (!st->num_sms) {
+  if (!st->num_sms) {  // first use of this state: kernel attributes, SMs
+    DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<4>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kPSmemBytes));
+    DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<2>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kPSmemBytes));
     int dev = 0;
     DBX_CUDA_TRY(cudaGetDevice(&dev));
     DBX_CUDA_TRY(cudaDeviceGetAttribute(&st->num_sms, cudaDevAttrMultiProcessorCount, dev));

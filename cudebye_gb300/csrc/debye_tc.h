@@ -32,6 +32,8 @@ struct TcState {  // cached plan data (basis, twiddles) and workspace
   int classes = 4;
   double rstep = 0;
   double *S_out = nullptr;  // optional: per-column row sums S[c][q]
+  PinArena *arena = nullptr;            // staging of the descriptor uploads
+  cudaStream_t alloc_stream = nullptr;  // stream-ordered growth (buf_grow)
 };
 
 // Host part: column tiles, descriptors uploaded, basis and twiddles for a

@@ -64,6 +64,31 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// Pinned host staging for host-to-device copies queued behind other work
+// on a stream: a copy from pageable memory makes the host wait for the
+// stream's earlier work, one from pinned memory does not. Space taken stays
+// valid until reset(), which the owner calls once the stream's earlier
+// copies are done (e.g. at the start of a server round on an idle lane).
+struct PinArena {
+  std::vector<std::pair<char *, size_t>> chunks;
+  size_t used = 0;  // bytes used in the last chunk
+  void *take(size_t n);  // n bytes, 16-byte aligned; nullptr if out of memory
+  void reset();          // one chunk of the total size, empty
+  void release();
+  PinArena() = default;
+  PinArena(const PinArena &) = delete;
+  PinArena &operator=(const PinArena &) = delete;
+  ~PinArena() { release(); }
+};
+// dst <- src (n bytes) on `stream`, through `arena` when it is not null.
+Error h2d_copy(void *dst, const void *src, size_t n, cudaStream_t stream,
+               PinArena *arena);
+// Grow b to at least `bytes` (contents not kept; *delta tracks the bytes
+// held). With `stream` the old buffer is freed and the new one allocated in
+// stream order, without a device synchronisation (for buffers used on that
+// stream only); without, cudaFree / cudaMalloc.
+Error buf_grow(DevBuf *b, size_t bytes, size_t *delta, cudaStream_t stream);
+
 // ---- resident model -------------------------------------------------------
 // Atoms are stored per species, each species sorted along a Morton curve
 // and cut into tiles of kTile atoms, so that a tile is spatially compact and
@@ -109,7 +134,8 @@ Error model_prepare(const float *x, const float *y, const float *z,
 size_t model_upload_bytes(const Model &m);
 // Copies max(natoms, 1) atoms; from pinned memory the copy is asynchronous
 // and `atoms` must stay untouched until it completes on `stream`.
-Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream);
+Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
+                      PinArena *arena = nullptr);
 size_t model_device_bytes(const Model &m);  // atoms, tiles, hist, plan
 void model_release(Model *m);
 
@@ -173,6 +199,11 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
                     double rstep, int64_t nbins, unsigned long long *out,
                     int64_t pitch, HistPlan *plan);
 void hist_plan_tasks(HistPlan *plan, int target_tasks);
+// Append a plan made for a model whose device arrays did not exist yet
+// (device pointers null, out = nullptr: output rows are byte offsets), with
+// the model's atoms, tiles and histogram base filled in.
+void hist_plan_append(HistPlan *plan, const HistPlan &part, const float4 *atoms,
+                      const int2 *tiles, unsigned long long *out);
 // clear + add + tasks for one model
 Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
                 int64_t nbins, unsigned long long *out, int64_t pitch,
@@ -180,6 +211,8 @@ Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
 
 struct HistWorkspace {  // device-side work lists and scratch
   DevBuf items, segs, tasks, rows, partial, oor;
+  PinArena *arena = nullptr;          // staging of the list uploads
+  cudaStream_t alloc_stream = nullptr;  // stream-ordered growth (buf_grow)
 };
 
 struct HistPlanCache {  // a plan and its uploaded work lists
@@ -227,6 +260,8 @@ struct PrefState {  // species and column descriptors of a batched prefactor
   DevBuf sp, colsp, f, fid;  // f: form factors [distinct set][q]; fid:
                              // species -> row of f, then row -> species
   int ncols = 0, nsp = 0;
+  PinArena *arena = nullptr;            // staging of the uploads
+  cudaStream_t alloc_stream = nullptr;  // stream-ordered growth (buf_grow)
 };
 // Upload species (concatenated) and per-column species pairs {a, b}; room
 // for the form factors of nq q values.

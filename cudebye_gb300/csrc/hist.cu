@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <thread>
 
 #include "engine.h"
@@ -424,7 +425,9 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
   const double inv = 1.0 / rstep;
   for (size_t pi = 0; pi < pairs.size(); ++pi) {
     const int a = pairs[pi].x, b = pairs[pi].y;
-    unsigned long long *row = out + (int64_t)pi * pitch;
+    // integer arithmetic: `out` may be null (a plan made before upload)
+    unsigned long long *row = reinterpret_cast<unsigned long long *>(
+        reinterpret_cast<uintptr_t>(out) + (uintptr_t)pi * pitch * sizeof(*out));
     plan->rows.push_back(HistRow{row, pitch});
     const int64_t na = m.sp_count[a], nb = m.sp_count[b];
     const int64_t block_pairs = (a == b) ? na * (na + 1) / 2 : na * nb;
@@ -636,6 +639,33 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
   for (size_t k = 0; k < order.size(); ++k) plan->tasks[k].next = order[k];
 }
 
+void hist_plan_append(HistPlan *plan, const HistPlan &part, const float4 *atoms,
+                      const int2 *tiles, unsigned long long *out) {
+  auto rebase = [&](unsigned long long *p) {
+    return reinterpret_cast<unsigned long long *>(reinterpret_cast<uintptr_t>(out) +
+                                                  reinterpret_cast<uintptr_t>(p));
+  };
+  const int ibase = (int)plan->items.size();
+  plan->items.insert(plan->items.end(), part.items.begin(), part.items.end());
+  plan->item_pairs.insert(plan->item_pairs.end(), part.item_pairs.begin(),
+                          part.item_pairs.end());
+  for (size_t i = 0; i < part.segs.size(); ++i) {
+    HistSeg s = part.segs[i];
+    s.atoms = atoms;
+    s.tiles = tiles;
+    s.out = rebase(s.out);
+    plan->segs.push_back(s);
+    int2 si = part.seg_items[i];
+    if (s.shape == kSegList) si = make_int2(si.x + ibase, si.y + ibase);
+    plan->seg_items.push_back(si);
+    plan->seg_pairs.push_back(part.seg_pairs[i]);
+  }
+  for (const HistRow &r : part.rows) plan->rows.push_back(HistRow{rebase(r.out), r.len});
+  plan->window = std::max(plan->window, part.window);
+  plan->nrows += part.nrows;
+  plan->pairs += part.pairs;
+}
+
 Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
                 int64_t nbins, unsigned long long *out, int64_t pitch,
                 int target_tasks, HistPlan *plan) {
@@ -645,45 +675,28 @@ Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
   return ok();
 }
 
-static Error ensure(DevBuf *b, size_t bytes, size_t *delta) {
-  if (b->bytes >= bytes) return ok();
-  if (b->p) {
-    cudaFree(b->p);
-    *delta -= b->bytes;
-    b->p = nullptr;
-    b->bytes = 0;
-  }
-  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
-  b->bytes = bytes;
-  *delta += bytes;
-  return ok();
-}
-
 Error hist_upload(const HistPlan &plan, HistWorkspace *ws, cudaStream_t stream,
                   size_t *ws_bytes_delta) {
   const int ntasks = (int)plan.tasks.size();
   const int nsegs = (int)plan.segs.size();
-  DBX_TRY(ensure(&ws->items, std::max<size_t>(plan.items.size(), 1) * sizeof(int2),
-                 ws_bytes_delta));
-  DBX_TRY(ensure(&ws->segs, std::max(nsegs, 1) * sizeof(HistSeg), ws_bytes_delta));
-  DBX_TRY(ensure(&ws->tasks, std::max(ntasks, 1) * sizeof(HistTask), ws_bytes_delta));
-  DBX_TRY(ensure(&ws->rows, std::max<size_t>(plan.rows.size(), 1) * sizeof(HistRow),
-                 ws_bytes_delta));
+  const cudaStream_t as = ws->alloc_stream;
+  DBX_TRY(buf_grow(&ws->items, std::max<size_t>(plan.items.size(), 1) * sizeof(int2),
+                   ws_bytes_delta, as));
+  DBX_TRY(buf_grow(&ws->segs, std::max(nsegs, 1) * sizeof(HistSeg), ws_bytes_delta, as));
+  DBX_TRY(buf_grow(&ws->tasks, std::max(ntasks, 1) * sizeof(HistTask), ws_bytes_delta, as));
+  DBX_TRY(buf_grow(&ws->rows, std::max<size_t>(plan.rows.size(), 1) * sizeof(HistRow),
+                   ws_bytes_delta, as));
   if (!plan.rows.empty())
-    DBX_CUDA_TRY(cudaMemcpyAsync(ws->rows.p, plan.rows.data(),
-                                 plan.rows.size() * sizeof(HistRow),
-                                 cudaMemcpyHostToDevice, stream));
+    DBX_TRY(h2d_copy(ws->rows.p, plan.rows.data(), plan.rows.size() * sizeof(HistRow),
+                     stream, ws->arena));
   if (ntasks == 0) return ok();
   if (!plan.items.empty())
-    DBX_CUDA_TRY(cudaMemcpyAsync(ws->items.p, plan.items.data(),
-                                 plan.items.size() * sizeof(int2),
-                                 cudaMemcpyHostToDevice, stream));
-  DBX_CUDA_TRY(cudaMemcpyAsync(ws->segs.p, plan.segs.data(),
-                               nsegs * sizeof(HistSeg), cudaMemcpyHostToDevice,
-                               stream));
-  DBX_CUDA_TRY(cudaMemcpyAsync(ws->tasks.p, plan.tasks.data(),
-                               ntasks * sizeof(HistTask),
-                               cudaMemcpyHostToDevice, stream));
+    DBX_TRY(h2d_copy(ws->items.p, plan.items.data(), plan.items.size() * sizeof(int2),
+                     stream, ws->arena));
+  DBX_TRY(h2d_copy(ws->segs.p, plan.segs.data(), nsegs * sizeof(HistSeg), stream,
+                   ws->arena));
+  DBX_TRY(h2d_copy(ws->tasks.p, plan.tasks.data(), ntasks * sizeof(HistTask), stream,
+                   ws->arena));
   return ok();
 }
 
@@ -692,10 +705,11 @@ Error hist_scratch(const HistPlan &plan, HistWorkspace *ws,
   int max_wl = 0;
   for (const HistSeg &s : plan.segs) max_wl = std::max(max_wl, s.wl);
   const int words = (max_wl + 1) / 2;
-  DBX_TRY(ensure(&ws->partial,
-                 std::max<size_t>((size_t)plan.tasks.size() * words, 1) * 4,
-                 ws_bytes_delta));
-  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
+  DBX_TRY(buf_grow(&ws->partial,
+                   std::max<size_t>((size_t)plan.tasks.size() * words, 1) * 4,
+                   ws_bytes_delta, ws->alloc_stream));
+  DBX_TRY(buf_grow(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta,
+                   ws->alloc_stream));
   // The tile kernel's shared-memory opt-in, once per device (kept out of
   // hist_launch so that a graph capture of it holds only stream work).
   static bool attr_done[64] = {false};
@@ -748,7 +762,8 @@ Error hist_launch(const HistPlan &plan, const HistWorkspace &lists,
 Error hist_plain(const Model &m, int row, int col, float inv_rstep,
                  int64_t nbins, unsigned long long *out, HistWorkspace *ws,
                  cudaStream_t stream, size_t *ws_bytes_delta) {
-  DBX_TRY(ensure(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta));
+  DBX_TRY(buf_grow(&ws->oor, 2 * sizeof(unsigned long long), ws_bytes_delta,
+                   ws->alloc_stream));
   DBX_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(unsigned long long) * nbins, stream));
   DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, 2 * sizeof(unsigned long long), stream));
   const int na = (int)m.sp_count[row], nb = (int)m.sp_count[col];

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <thread>
 #include <vector>
 
@@ -142,12 +143,81 @@ Error model_prepare(const float *x, const float *y, const float *z,
   return ok();
 }
 
+void *PinArena::take(size_t n) {
+  n = (n + 15) & ~size_t(15);
+  if (!chunks.empty() && used + n <= chunks.back().second) {
+    void *p = chunks.back().first + used;
+    used += n;
+    return p;
+  }
+  size_t total = 0;
+  for (auto &c : chunks) total += c.second;
+  const size_t cap = std::max(n, std::max<size_t>(total, size_t(8) << 20));
+  char *p = nullptr;
+  if (cudaMallocHost((void **)&p, cap) != cudaSuccess) return nullptr;
+  chunks.emplace_back(p, cap);
+  used = n;
+  return p;
+}
+
+void PinArena::reset() {
+  if (chunks.size() > 1) {
+    size_t total = 0;
+    for (auto &c : chunks) total += c.second;
+    release();
+    char *p = nullptr;
+    if (cudaMallocHost((void **)&p, total) == cudaSuccess) chunks.emplace_back(p, total);
+  }
+  used = 0;
+}
+
+void PinArena::release() {
+  for (auto &c : chunks) cudaFreeHost(c.first);
+  chunks.clear();
+  used = 0;
+}
+
+Error h2d_copy(void *dst, const void *src, size_t n, cudaStream_t stream,
+               PinArena *arena) {
+  if (n == 0) return ok();
+  const void *from = src;
+  if (arena) {
+    if (void *p = arena->take(n)) {
+      std::memcpy(p, src, n);
+      from = p;
+    }
+  }
+  DBX_CUDA_TRY(cudaMemcpyAsync(dst, from, n, cudaMemcpyHostToDevice, stream));
+  return ok();
+}
+
+Error buf_grow(DevBuf *b, size_t bytes, size_t *delta, cudaStream_t stream) {
+  if (b->bytes >= bytes) return ok();
+  if (b->p) {
+    if (stream)
+      cudaFreeAsync(b->p, stream);
+    else
+      cudaFree(b->p);
+    *delta -= b->bytes;
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  if (stream)
+    DBX_CUDA_TRY(cudaMallocAsync(&b->p, bytes, stream));
+  else
+    DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
+  b->bytes = bytes;
+  *delta += bytes;
+  return ok();
+}
+
 size_t model_upload_bytes(const Model &m) {
   return sizeof(float4) * std::max<int64_t>(m.natoms, 1) +
          sizeof(int2) * std::max<size_t>(m.tiles.size(), 1);
 }
 
-Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream) {
+Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
+                      PinArena *arena) {
   const size_t abytes = sizeof(float4) * std::max<int64_t>(m->natoms, 1);
   const size_t tbytes = sizeof(int2) * std::max<size_t>(m->tiles.size(), 1);
   if (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
@@ -157,9 +227,8 @@ Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream) {
   DBX_CUDA_TRY(cudaMemcpyAsync(m->d_atoms, atoms, abytes,
                                cudaMemcpyHostToDevice, stream));
   if (!m->tiles.empty())
-    DBX_CUDA_TRY(cudaMemcpyAsync(m->d_tiles, m->tiles.data(),
-                                 sizeof(int2) * m->tiles.size(),
-                                 cudaMemcpyHostToDevice, stream));
+    DBX_TRY(h2d_copy(m->d_tiles, m->tiles.data(), sizeof(int2) * m->tiles.size(),
+                     stream, arena));
   return ok();
 }
 

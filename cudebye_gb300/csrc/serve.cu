@@ -68,6 +68,12 @@ struct Req {
   double t_submit = 0, t_done = 0;
   size_t offset = 0;  // of I in the lane's result buffer
   bool solo = false;  // retried alone after its round failed
+  // host preparation of a new model, done by a preparation thread before
+  // the request is queued: its sorted atoms, its host part (tiles, boxes,
+  // species ranges) and its histogram plan without device pointers
+  std::unique_ptr<Model> hm;
+  std::vector<float4> atoms;
+  HistPlan part;
 };
 
 struct SModel {  // a resident model of the server
@@ -84,6 +90,9 @@ struct SModel {  // a resident model of the server
 
 struct Lane {
   cudaStream_t stream = nullptr;
+  // pinned staging of the round's host-to-device copies, so that queueing
+  // a request's work behind the histogram launch never waits for it
+  PinArena arena;
   HistWorkspace hws;  // work lists and scratch of the round's histograms
   HistPlan plan;
   TcState tc;
@@ -94,20 +103,6 @@ struct Lane {
   std::vector<Req *> reqs;
   bool busy = false;
 };
-
-Error grow(DevBuf *b, size_t bytes, size_t *used) {
-  if (b->bytes >= bytes) return ok();
-  if (b->p) {
-    cudaFree(b->p);
-    *used -= b->bytes;
-    b->p = nullptr;
-    b->bytes = 0;
-  }
-  DBX_CUDA_TRY(cudaMalloc(&b->p, bytes));
-  b->bytes = bytes;
-  *used += bytes;
-  return ok();
-}
 
 void release(DevBuf *b) {
   if (b->p) cudaFree(b->p);
@@ -141,7 +136,11 @@ struct dbx_server {
   int hist_tasks = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<dbx::Req *> queue;
+  std::deque<dbx::Req *> queue;     // ready for admission
+  std::deque<dbx::Req *> prep_q;    // new models waiting for host preparation
+  std::condition_variable cv_prep;
+  int prepping = 0;                 // preparations in progress
+  std::vector<std::thread> preps;
   std::map<int64_t, std::unique_ptr<dbx::Req>> reqs;  // by ticket
   std::map<int64_t, dbx::SModel> models;              // worker thread only
   int64_t next_ticket = 1, next_model = 1;
@@ -265,18 +264,21 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
   L.busy = true;
   const cudaStream_t st = L.stream;
   size_t used_delta = 0;
+  L.arena.reset();  // the lane is idle: its previous round's copies are done
   // 1. new models: sort + upload, histogram buffers
   std::vector<int64_t> new_ids;
   for (Req *r : batch) {
     if (r->kind != kNew) continue;
-    auto m = std::make_unique<Model>();
-    int64_t natoms = 0;
-    for (int64_t c : r->counts) natoms += std::max<int64_t>(c, 0);
-    // pageable: the copy is staged before cudaMemcpyAsync returns
-    std::vector<float4> atoms(std::max<int64_t>(natoms, 1));
-    DBX_TRY(model_prepare(r->x.data(), r->y.data(), r->z.data(), r->counts.data(),
-                          (int)r->counts.size(), m.get(), atoms.data()));
-    DBX_TRY(model_to_device(m.get(), atoms.data(), st));
+    // host part prepared by a preparation thread; atoms through the pinned
+    // staging (pageable as a fallback)
+    auto m = std::make_unique<Model>(*r->hm);
+    const size_t abytes = sizeof(float4) * r->atoms.size();
+    const float4 *atoms = r->atoms.data();
+    if (void *p = L.arena.take(abytes)) {
+      std::memcpy(p, atoms, abytes);
+      atoms = (const float4 *)p;
+    }
+    DBX_TRY(model_to_device(m.get(), atoms, st, &L.arena));
     m->hist_pitch = pitch_of(r->nbins);
     m->hist_bytes = hist_bytes(m->nspecies, r->nbins);
     DBX_CUDA_TRY(cudaMalloc(&m->d_hist, m->hist_bytes));
@@ -297,13 +299,10 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
   Timers off;
   hist_plan_clear(&L.plan);
   double rstep = 0;
-  for (int64_t id : new_ids) {
-    SModel &sm = s->models[id];
-    std::vector<int2> pairs;
-    for (int a = 0; a < sm.m->nspecies; ++a)
-      for (int b = a; b < sm.m->nspecies; ++b) pairs.push_back(make_int2(a, b));
-    DBX_TRY(hist_plan_add(*sm.m, pairs, sm.rstep, sm.nbins, sm.m->d_hist,
-                          sm.m->hist_pitch, &L.plan));
+  for (Req *r : batch) {
+    if (r->kind != kNew) continue;
+    SModel &sm = s->models[r->model_out];
+    hist_plan_append(&L.plan, r->part, sm.m->d_atoms, sm.m->d_tiles, sm.m->d_hist);
     rstep = sm.rstep;
   }
   hist_plan_tasks(&L.plan, s->hist_tasks);
@@ -321,7 +320,7 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
     r->offset = total;
     total += r->K.size();
   }
-  DBX_TRY(grow(&L.I, std::max<size_t>(total, 1) * 8, &s->used));
+  DBX_TRY(buf_grow(&L.I, std::max<size_t>(total, 1) * 8, &s->used, st));
   if (L.hI_bytes < total * 8) {
     if (L.hI) cudaFreeHost(L.hI);
     L.hI = nullptr;
@@ -332,10 +331,9 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
     const int64_t id = r->model ? r->model : r->model_out;
     SModel &sm = s->models[id];
     const int P = sm.m->nspecies, np = npairs_of(P), nq = (int)r->K.size();
-    DBX_TRY(grow(&L.K, (size_t)nq * 8, &s->used));
-    DBX_TRY(grow(&L.ff, (size_t)np * nq * 8, &s->used));
-    DBX_CUDA_TRY(cudaMemcpyAsync(L.K.p, r->K.data(), (size_t)nq * 8,
-                                 cudaMemcpyHostToDevice, st));
+    DBX_TRY(buf_grow(&L.K, (size_t)nq * 8, &s->used, st));
+    DBX_TRY(buf_grow(&L.ff, (size_t)np * nq * 8, &s->used, st));
+    DBX_TRY(h2d_copy(L.K.p, r->K.data(), (size_t)nq * 8, st, &L.arena));
     std::vector<int2> col_sp;
     for (int a = 0; a < P; ++a)
       for (int b = a; b < P; ++b) col_sp.push_back(make_int2(a, b));
@@ -447,6 +445,53 @@ void finish_round(dbx_server *s, Lane &L, const Error &launch_err) {
   s->cv_done.notify_all();
 }
 
+// Host preparation of a new model: spatial sort, tiles and the histogram
+// plan (preparation thread, no lock).
+Error prepare(Req *r) {
+  const int P = (int)r->counts.size();
+  int64_t natoms = 0;
+  for (int64_t c : r->counts) natoms += c;
+  r->hm = std::make_unique<Model>();
+  r->atoms.resize(std::max<int64_t>(natoms, 1));
+  DBX_TRY(model_prepare(r->x.data(), r->y.data(), r->z.data(), r->counts.data(), P,
+                        r->hm.get(), r->atoms.data()));
+  std::vector<int2> pairs;
+  for (int a = 0; a < P; ++a)
+    for (int b = a; b < P; ++b) pairs.push_back(make_int2(a, b));
+  hist_plan_clear(&r->part);
+  DBX_TRY(hist_plan_add(*r->hm, pairs, r->rstep, r->nbins, nullptr, pitch_of(r->nbins),
+                        &r->part));
+  // the coordinates are in r->atoms now
+  std::vector<float>().swap(r->x);
+  std::vector<float>().swap(r->y);
+  std::vector<float>().swap(r->z);
+  return ok();
+}
+
+void prep_main(dbx_server *s) {
+  for (;;) {
+    Req *r = nullptr;
+    {
+      std::unique_lock<std::mutex> lock(s->mu);
+      s->cv_prep.wait(lock, [&] { return s->stop || !s->prep_q.empty(); });
+      if (s->prep_q.empty()) return;  // stopping, nothing left
+      r = s->prep_q.front();
+      s->prep_q.pop_front();
+      ++s->prepping;
+    }
+    Error e = prepare(r);
+    std::lock_guard<std::mutex> lock(s->mu);
+    --s->prepping;
+    if (e.code) {
+      complete(s, r, e.code, e.msg);
+      s->cv_done.notify_all();
+    } else {
+      s->queue.push_back(r);
+    }
+    s->cv_work.notify_all();
+  }
+}
+
 void worker_main(dbx_server *s) {
   cudaSetDevice(s->device);
   int order[2] = {0, 1};  // lanes in launch order (oldest first)
@@ -461,9 +506,13 @@ void worker_main(dbx_server *s) {
     {
       std::unique_lock<std::mutex> lock(s->mu);
       any_busy = s->lanes[0].busy || s->lanes[1].busy;
-      if (s->stop && s->queue.empty() && !any_busy) return;
+      const bool prep_idle = s->prep_q.empty() && s->prepping == 0;
+      if (s->stop && s->queue.empty() && !any_busy && prep_idle) return;
       if (s->queue.empty() && !any_busy) {
-        s->cv_work.wait(lock, [&] { return s->stop || !s->queue.empty(); });
+        s->cv_work.wait(lock, [&] {
+          return (s->stop && s->prep_q.empty() && s->prepping == 0) ||
+                 !s->queue.empty();
+        });
         continue;
       }
       for (int k = 0; k < 2; ++k)
@@ -518,11 +567,20 @@ int dbx_server_create(dbx_server **out, int device, size_t budget) {
                              device) != cudaSuccess)
     return DBX_ERR_CUDA;
   s->hist_tasks = 4 * s->num_sms;
-  for (dbx::Lane &L : s->lanes)
+  for (dbx::Lane &L : s->lanes) {
     if (cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking) != cudaSuccess)
       return DBX_ERR_CUDA;
+    // lane workspaces grow in the lane's stream order (no device-wide
+    // synchronisation while the other lane computes)
+    L.hws.arena = L.tc.arena = L.pref.arena = &L.arena;
+    L.hws.alloc_stream = L.tc.alloc_stream = L.pref.alloc_stream = L.stream;
+  }
   dbx_server *raw = s.get();
   s->worker = std::thread(dbx::worker_main, raw);
+  // host preparation (sort, plan) of new models runs beside the worker
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  for (unsigned i = 0; i < std::min(4u, std::max(1u, hw / 4)); ++i)
+    s->preps.emplace_back(dbx::prep_main, raw);
   *out = s.release();
   return DBX_OK;
 }
@@ -555,9 +613,14 @@ int dbx_server_submit(dbx_server *s, const dbx_request *q, int64_t *ticket) {
   if (s->stop) return DBX_ERR_ARG;
   r->ticket = s->next_ticket++;
   *ticket = r->ticket;
-  s->queue.push_back(r.get());
+  if (r->model) {  // re-scoring: straight to admission
+    s->queue.push_back(r.get());
+    s->cv_work.notify_one();
+  } else {
+    s->prep_q.push_back(r.get());
+    s->cv_prep.notify_one();
+  }
   s->reqs[r->ticket] = std::move(r);
-  s->cv_work.notify_one();
   return DBX_OK;
 }
 
@@ -600,7 +663,10 @@ int dbx_server_destroy(dbx_server *s) {
     std::lock_guard<std::mutex> lock(s->mu);
     s->stop = true;
   }
+  s->cv_prep.notify_all();
   s->cv_work.notify_all();
+  for (std::thread &t : s->preps)
+    if (t.joinable()) t.join();
   if (s->worker.joinable()) s->worker.join();
   cudaSetDevice(s->device);
   for (auto &kv : s->models) {
