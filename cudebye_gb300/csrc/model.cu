@@ -220,9 +220,13 @@ Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
                       PinArena *arena) {
   const size_t abytes = sizeof(float4) * std::max<int64_t>(m->natoms, 1);
   const size_t tbytes = sizeof(int2) * std::max<size_t>(m->tiles.size(), 1);
-  if (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
-      cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess)
-    return fail(DBX_ERR_NOMEM, "cudaMalloc failed for model");
+  // with a staging arena (a server lane) the arrays are allocated in the
+  // stream's order, without waiting for other streams
+  if (arena ? (cudaMallocAsync(&m->d_atoms, abytes, stream) != cudaSuccess ||
+               cudaMallocAsync(&m->d_tiles, tbytes, stream) != cudaSuccess)
+            : (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
+               cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess))
+    return fail(DBX_ERR_NOMEM, "device allocation failed for model");
   m->dev_bytes = abytes + tbytes;
   DBX_CUDA_TRY(cudaMemcpyAsync(m->d_atoms, atoms, abytes,
                                cudaMemcpyHostToDevice, stream));

@@ -98,8 +98,7 @@ struct Lane {
   TcState tc;
   PrefState pref;
   DevBuf K, ff, I;
-  double *hI = nullptr;  // pinned results
-  size_t hI_bytes = 0;
+  double *hI = nullptr;  // the round's results (pinned, in the arena)
   std::vector<Req *> reqs;
   bool busy = false;
 };
@@ -281,7 +280,7 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
     DBX_TRY(model_to_device(m.get(), atoms, st, &L.arena));
     m->hist_pitch = pitch_of(r->nbins);
     m->hist_bytes = hist_bytes(m->nspecies, r->nbins);
-    DBX_CUDA_TRY(cudaMalloc(&m->d_hist, m->hist_bytes));
+    DBX_CUDA_TRY(cudaMallocAsync(&m->d_hist, m->hist_bytes, st));
     const int64_t id = s->next_model++;
     m->id = id;
     SModel sm;
@@ -321,12 +320,8 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
     total += r->K.size();
   }
   DBX_TRY(buf_grow(&L.I, std::max<size_t>(total, 1) * 8, &s->used, st));
-  if (L.hI_bytes < total * 8) {
-    if (L.hI) cudaFreeHost(L.hI);
-    L.hI = nullptr;
-    DBX_CUDA_TRY(cudaMallocHost((void **)&L.hI, std::max<size_t>(total, 1) * 8));
-    L.hI_bytes = std::max<size_t>(total, 1) * 8;
-  }
+  L.hI = (double *)L.arena.take(std::max<size_t>(total, 1) * 8);
+  if (!L.hI) return fail(DBX_ERR_NOMEM, "pinned host memory for results");
   for (Req *r : batch) {
     const int64_t id = r->model ? r->model : r->model_out;
     SModel &sm = s->models[id];
@@ -347,7 +342,7 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
       if (sm.S.bytes < (size_t)np * nq * 8) {
         s->used -= sm.S.bytes;
         release(&sm.S);
-        DBX_CUDA_TRY(cudaMalloc(&sm.S.p, (size_t)np * nq * 8));
+        DBX_CUDA_TRY(cudaMallocAsync(&sm.S.p, (size_t)np * nq * 8, st));
         sm.S.bytes = (size_t)np * nq * 8;
         s->used += sm.S.bytes;
       }
@@ -573,6 +568,8 @@ int dbx_server_create(dbx_server **out, int device, size_t budget) {
     // lane workspaces grow in the lane's stream order (no device-wide
     // synchronisation while the other lane computes)
     L.hws.arena = L.tc.arena = L.pref.arena = &L.arena;
+    L.arena.take(size_t(64) << 20);  // initial capacity (grows when needed)
+    L.arena.reset();
     L.hws.alloc_stream = L.tc.alloc_stream = L.pref.alloc_stream = L.stream;
   }
   dbx_server *raw = s.get();
@@ -679,7 +676,6 @@ int dbx_server_destroy(dbx_server *s) {
                            &L.K, &L.ff, &L.I})
       dbx::release(b);
     dbx::tc_release(&L.tc);
-    if (L.hI) cudaFreeHost(L.hI);
     if (L.stream) cudaStreamDestroy(L.stream);
   }
   delete s;
