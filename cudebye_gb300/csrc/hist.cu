@@ -565,7 +565,10 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       s.kb = (int)(w * W);
       s.wl = (int)std::min<int64_t>(W, nbins - w * W);
       s.task_begin = s.task_end = 0;
-      s.nbins = (unsigned)nbins;
+      // a tile pair listed in several windows has its out-of-range pairs
+      // counted by the last window only: the others get an unreachable
+      // bound (no distance bins at or beyond 2^32 - 1 in the test)
+      s.nbins = w == nwin - 1 ? (unsigned)nbins : 0xFFFFFFFFu;
       s.shape = kSegList;
       s.ti0 = s.tni = s.tj0 = s.tnj = 0;
       plan->segs.push_back(s);

@@ -199,6 +199,41 @@ def test_out_of_range_is_an_error(engine):
         m.free()
 
 
+def test_out_of_range_count_many_windows(orc):
+    """A fine-binned histogram of several windows whose rmax is half the
+    particle's extent: the range error reports exactly the oracle's count
+    of distances beyond rmax (each counted once, although their tile pairs
+    reach several windows)."""
+    code = r"""
+import numpy as np, re, sys
+sys.path.insert(0, %r)
+import cudebye_gb300 as cd
+from cudebye_gb300 import lattice
+from oracle import pyoracle as orc
+m = lattice.spinel(radius=12.0, target=900, seed=17, rstep=3e-5)
+nbins = cd.channels(m.rmax / 2, 3e-5)
+assert nbins > 3 * 114688
+with cd.Engine(0) as e:
+    mod = e.upload(m.xyz, m.counts)
+    try:
+        e.histogram(mod, 3e-5, nbins)
+        raise SystemExit("no range error")
+    except cd.DebyeError as err:
+        assert err.code == -7, err
+        got = int(re.search(r"(\d+) distances", str(err)).group(1))
+    _, bad = orc.model_histograms(m.xyz, m.counts, 3e-5, nbins)
+    assert got == bad > 0, (got, bad)
+    h = e.histogram(mod, 3e-5, cd.channels(m.rmax, 3e-5))
+    want, bad = orc.model_histograms(m.xyz, m.counts, 3e-5, cd.channels(m.rmax, 3e-5))
+    assert bad == 0
+    np.testing.assert_array_equal(h, want)
+print("OK")
+""" % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run(["python", "-c", code], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
 def test_bad_arguments(engine):
     m = engine.upload(np.zeros((2, 3), np.float32), [2])
     stale = cd.Model(engine, m.id, m.counts)
