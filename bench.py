@@ -49,10 +49,11 @@ def measured_traffic(kernel, workload):
 
 def launches_per_pattern(mode, npairs):
     """Kernels one dbx_pattern call launches on a resident model whose q grid
-    is unchanged: the histogram (zero, tiles, reduce), the prefactor, then
-    for the tensor-core sum the self term, weights, contraction and reduce,
-    for the direct sums one launch per 16 pair types."""
-    n = 3 + 1
+    is unchanged: the histogram (zero, tiles, reduce), the prefactor (form
+    factors, pair products), then for the tensor-core sum the self term,
+    weights, contraction and reduce, for the direct sums one launch per 16
+    pair types."""
+    n = 3 + 2
     if mode == "tc":
         return n + 4
     return n + (npairs + 15) // 16
