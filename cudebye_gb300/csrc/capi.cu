@@ -141,6 +141,7 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
       for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
     m->plan_rstep = 0;
     m->plan_nbins = 0;
+    if (nbins > dbx::hist_window_bins()) DBX_TRY(dbx::model_host_boxes(m, c->stream));
     DBX_TRY(dbx::hist_plan(*m, pairs, rstep, nbins, m->d_hist, pitch,
                            c->hist_tasks, &m->plan_cache->plan));
     const size_t before = delta;
@@ -359,6 +360,8 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
       std::vector<int2> pairs;
       for (int r = 0; r < m->nspecies; ++r)
         for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
+      if (nbins[i] > dbx::hist_window_bins())
+        DBX_TRY(dbx::model_host_boxes(m, c->stream));
       DBX_TRY(dbx::hist_plan_add(*m, pairs, rstep, nbins[i], m->d_hist,
                                  m->hist_pitch, &b.hp.plan));
     }
@@ -612,12 +615,32 @@ int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
   if (!c->pin_ev &&
       cudaEventCreateWithFlags(&c->pin_ev, cudaEventDisableTiming) != cudaSuccess)
     return set_err(c, dbx::fail(DBX_ERR_CUDA, "cudaEventCreate failed"));
-  Error e = dbx::model_prepare(x, y, z, counts, nspecies, m.get(), c->pin);
-  if (e.code) return set_err(c, e);
-  const size_t need = dbx::model_upload_bytes(*m);
+  // Large models are sorted on the device (same order as the host sort,
+  // which would dominate their upload); DBX_DEVICE_SORT_MIN sets the size.
+  static const int64_t dev_min = [] {
+    const char *v = getenv("DBX_DEVICE_SORT_MIN");
+    return v ? std::max<int64_t>(1, atoll(v)) : int64_t(32768);
+  }();
+  Error e;
+  for (int s = 0; s < nspecies; ++s)
+    if (counts[s] < 0) return set_err(c, dbx::fail(DBX_ERR_ARG, "negative species count"));
+  if (natoms > 0 && (!x || !y || !z))
+    return set_err(c, dbx::fail(DBX_ERR_ARG, "null coordinate array"));
+  if (natoms >= (int64_t(1) << 31))
+    return set_err(c, dbx::fail(DBX_ERR_ARG, "more than 2^31 atoms"));
+  const int64_t ntiles_est = natoms / dbx::kTile + nspecies;
+  const size_t need = sizeof(float4) * n + (sizeof(int2) + sizeof(dbx::TileBox)) *
+                                               (size_t)std::max<int64_t>(ntiles_est, 1);
   if (c->budget && c->used + need > c->budget)
     return set_err(c, dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by model"));
-  e = dbx::model_to_device(m.get(), c->pin, c->stream);
+  if (natoms >= dev_min) {
+    e = dbx::model_upload_sorted(m.get(), x, y, z, counts, nspecies, (float *)c->pin,
+                                 c->stream);
+  } else {
+    e = dbx::model_prepare(x, y, z, counts, nspecies, m.get(), c->pin);
+    if (e.code) return set_err(c, e);
+    e = dbx::model_to_device(m.get(), c->pin, c->stream);
+  }
   if (e.code) {
     dbx::model_release(m.get());
     return set_err(c, e);
@@ -626,7 +649,13 @@ int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
     return set_err(c, dbx::fail(DBX_ERR_CUDA, "cudaEventRecord failed"));
   c->pin_used = true;
   c->used += m->dev_bytes;
-  c->h2d += m->dev_bytes;
+  // bytes copied: sorted atoms, tiles (host sort) or raw coordinates,
+  // tiles and the species descriptors (device sort)
+  c->h2d += natoms >= dev_min
+                ? (int64_t)(12 * natoms + sizeof(int2) * m->tiles.size() +
+                            (6 * sizeof(unsigned) + sizeof(long long) + sizeof(int)) *
+                                nspecies + sizeof(long long))
+                : (int64_t)m->dev_bytes;
   m->id = c->next_id++;
   *model_id = m->id;
   c->models[m->id] = std::move(m);
@@ -660,6 +689,10 @@ int dbx_pair_histogram(dbx_ctx *c, int64_t id, int row, int col, double rstep,
   Error e = grow(c, &c->tmp_hist, sizeof(unsigned long long) * pitch);
   if (e.code) return set_err(c, e);
   dbx::HistPlan plan;
+  if (nbins > dbx::hist_window_bins()) {
+    e = dbx::model_host_boxes(m, c->stream);
+    if (e.code) return set_err(c, e);
+  }
   e = dbx::hist_plan(*m, {make_int2(row, col)}, rstep, nbins,
                      (unsigned long long *)c->tmp_hist.p, pitch, c->hist_tasks,
                      &plan);

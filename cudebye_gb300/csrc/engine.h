@@ -106,9 +106,11 @@ struct Model {
   std::vector<int64_t> sp_start, sp_count;  // in atoms (sorted layout)
   std::vector<int> tile_start;              // first tile of each species (+ end)
   std::vector<int2> tiles;                  // {first atom, count}
-  std::vector<TileBox> boxes;               // per tile, host only
+  std::vector<TileBox> boxes;               // per tile (host; for device-
+                                            // sorted models filled on demand)
   float4 *d_atoms = nullptr;                // natoms x (x, y, z, 0)
   int2 *d_tiles = nullptr;
+  TileBox *d_boxes = nullptr;               // per tile (device-sorted models)
   size_t dev_bytes = 0;
   // Cached histogram plan of all pairs for (plan_rstep, plan_nbins): the
   // work lists depend only on the geometry and the binning.
@@ -137,6 +139,15 @@ size_t model_upload_bytes(const Model &m);
 Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
                       PinArena *arena = nullptr);
 size_t model_device_bytes(const Model &m);  // atoms, tiles, hist, plan
+// Sort and upload on the device (morton.cu): the same atoms, tiles and
+// boxes as model_prepare + model_to_device; `pin` is pinned host memory
+// of at least 3 natoms floats; the tile boxes stay on the device
+// (d_boxes) until model_host_boxes copies them for a multi-window plan.
+// For natoms > 0.
+Error model_upload_sorted(Model *m, const float *x, const float *y, const float *z,
+                          const int64_t *counts, int nspecies, float *pin,
+                          cudaStream_t stream);
+Error model_host_boxes(Model *m, cudaStream_t stream);
 void model_release(Model *m);
 
 inline int npairs_of(int p) { return p * (p + 1) / 2; }

@@ -461,6 +461,8 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       plan->nrows += 1;
       continue;
     }
+    if (m.boxes.size() != m.tiles.size())
+      return fail(DBX_ERR_ARG, "tile boxes are not on the host");
     // Tile pairs listed per window from their bounding boxes, rows of tiles
     // split among host threads by item count; the lists are joined in row
     // order, so the plan does not depend on the thread count.

@@ -243,6 +243,7 @@ size_t model_device_bytes(const Model &m) {
 void model_release(Model *m) {
   if (m->d_atoms) cudaFree(m->d_atoms);
   if (m->d_tiles) cudaFree(m->d_tiles);
+  if (m->d_boxes) cudaFree(m->d_boxes);
   if (m->d_hist) cudaFree(m->d_hist);
   if (m->plan_cache) {
     for (DevBuf *b : {&m->plan_cache->lists.items, &m->plan_cache->lists.segs,
@@ -253,6 +254,7 @@ void model_release(Model *m) {
   }
   m->d_atoms = nullptr;
   m->d_tiles = nullptr;
+  m->d_boxes = nullptr;
   m->d_hist = nullptr;
   m->dev_bytes = m->hist_bytes = m->plan_bytes = 0;
 }

@@ -1,0 +1,389 @@
+// morton.cu — the spatial sort of a model's atoms on the device.
+//
+// The same order as the host path (model_prepare): per species, Morton
+// codes on a grid over the species' bounding cube with about 2 cells per
+// atom, sorted stably (equal codes keep their input order), so a model
+// uploaded either way has the same atoms, tiles and boxes. Used by
+// dbx_model_upload for large models, where the host sort would dominate
+// the upload: raw coordinates go to the device once and the codes, the
+// radix sort (LSD, 8-bit digits, stable), the gather into float4 atoms and
+// the tile bounding boxes run there.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "engine.h"
+
+namespace dbx {
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortChunk = 4096;  // keys per block and pass (16 per thread)
+constexpr int kRadix = 256;
+
+__device__ __forceinline__ uint32_t spread10_d(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+// Species of global atom index i (species ranges start[0..ns]).
+__device__ __forceinline__ int species_of(long long i, const long long *start,
+                                          int ns) {
+  int s = 0;
+  while (s + 1 < ns && i >= start[s + 1]) ++s;
+  return s;
+}
+
+// Per species, per block: min and max of x, y, z over the block's share;
+// combined by atomics on order-preserving integer images of the floats
+// (NaN coordinates are skipped, as std::min / std::max skip them on the
+// host when the running value comes first).
+__device__ __forceinline__ unsigned f2ord(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned o) {
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
+}
+
+__global__ void bbox_kernel(const float *__restrict__ xyz, long long n,
+                            const long long *__restrict__ start, int ns,
+                            unsigned *__restrict__ lohi /* [ns][6] */) {
+  const int s = blockIdx.y;
+  const long long b = start[s], e = start[s + 1];
+  unsigned lo[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, hi[3] = {0u, 0u, 0u};
+  for (long long i = b + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < e;
+       i += (long long)gridDim.x * blockDim.x) {
+    for (int d = 0; d < 3; ++d) {
+      const float v = xyz[d * n + i];
+      if (v != v) continue;  // NaN
+      const unsigned o = f2ord(v);
+      lo[d] = min(lo[d], o);
+      hi[d] = max(hi[d], o);
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    for (int off = 16; off > 0; off >>= 1) {
+      lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+      hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&lohi[s * 6 + d], lo[d]);
+      atomicMax(&lohi[s * 6 + 3 + d], hi[d]);
+    }
+  }
+}
+
+// Morton key of every atom: bits 32.. the species, bits 0..31 the code
+// computed exactly as the host does (FP32, IEEE operations).
+__global__ void keys_kernel(const float *__restrict__ xyz, long long n,
+                            const long long *__restrict__ start, int ns,
+                            const unsigned *__restrict__ lohi,
+                            const int *__restrict__ bits,
+                            unsigned long long *__restrict__ key,
+                            int *__restrict__ idx) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = species_of(i, start, ns);
+  float lo[3], ext = 0.f;
+  for (int d = 0; d < 3; ++d) {
+    const unsigned l = lohi[s * 6 + d], h = lohi[s * 6 + 3 + d];
+    // an all-NaN axis has no extent (the host's running min stays +inf)
+    lo[d] = l == 0xFFFFFFFFu ? INFINITY : ord2f(l);
+    const float hv = h == 0u ? -INFINITY : ord2f(h);
+    ext = fmaxf(ext, __fsub_rn(hv, lo[d]));
+  }
+  const float top = (float)((1u << bits[s]) - 1);
+  const float scale = ext > 0 ? __fdiv_rn(top, ext) : 0.f;
+  uint32_t q[3];
+  for (int d = 0; d < 3; ++d) {
+    float t = __fmul_rn(__fsub_rn(xyz[d * n + i], lo[d]), scale);
+    t = t >= 0.f ? (t <= top ? t : top) : 0.f;  // NaN -> 0
+    q[d] = (uint32_t)t;
+  }
+  const uint32_t code =
+      spread10_d(q[0]) | (spread10_d(q[1]) << 1) | (spread10_d(q[2]) << 2);
+  key[i] = ((unsigned long long)s << 32) | code;
+  idx[i] = (int)(i - start[s]);
+}
+
+// Digit counts of each block's chunk: cnt[digit * nblocks + block].
+__global__ void radix_count_kernel(const unsigned long long *__restrict__ key,
+                                   long long n, int shift,
+                                   unsigned *__restrict__ cnt) {
+  __shared__ unsigned h[kRadix];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kSortChunk;
+  for (int k = threadIdx.x; k < kSortChunk; k += kSortThreads) {
+    const long long i = base + k;
+    if (i < n) atomicAdd(&h[(key[i] >> shift) & 0xFF], 1u);
+  }
+  __syncthreads();
+  cnt[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive prefix sum of m counts in place (one block).
+__global__ void radix_scan_kernel(unsigned *__restrict__ cnt, long long m) {
+  __shared__ unsigned long long part[1024];
+  const int t = threadIdx.x;
+  const long long per = (m + blockDim.x - 1) / blockDim.x;
+  const long long b = t * per, e = b + per < m ? b + per : m;
+  unsigned long long s = 0;
+  for (long long i = b; i < e; ++i) s += cnt[i];
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+    const unsigned long long v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  unsigned long long acc = part[t] - s;  // exclusive
+  for (long long i = b; i < e; ++i) {
+    const unsigned c = cnt[i];
+    cnt[i] = (unsigned)acc;
+    acc += c;
+  }
+}
+
+// Stable scatter of each block's chunk: warp w takes its 512 keys in
+// order, 32 at a time; lanes with equal digits are ranked by lane, and the
+// warps' offsets per digit follow the warps' order.
+__global__ void radix_scatter_kernel(const unsigned long long *__restrict__ key,
+                                     const int *__restrict__ idx, long long n,
+                                     int shift, const unsigned *__restrict__ cnt,
+                                     unsigned long long *__restrict__ key2,
+                                     int *__restrict__ idx2) {
+  constexpr int kWarps = kSortThreads / 32;
+  constexpr int kPerWarp = kSortChunk / kWarps;
+  __shared__ unsigned wh[kWarps][kRadix];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < kWarps * kRadix; i += kSortThreads)
+    (&wh[0][0])[i] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kSortChunk + warp * kPerWarp;
+  for (int k = lane; k < kPerWarp; k += 32) {
+    const long long i = base + k;
+    if (i < n) atomicAdd(&wh[warp][(key[i] >> shift) & 0xFF], 1u);
+  }
+  __syncthreads();
+  // offsets: global offset of (digit, block) + counts of earlier warps
+  {
+    const int d = threadIdx.x;  // kSortThreads == kRadix
+    unsigned off = cnt[(size_t)d * gridDim.x + blockIdx.x];
+    for (int w = 0; w < kWarps; ++w) {
+      const unsigned c = wh[w][d];
+      wh[w][d] = off;
+      off += c;
+    }
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  for (int k0 = 0; k0 < kPerWarp; k0 += 32) {
+    const long long i = base + k0 + lane;
+    const bool valid = i < n;
+    // invalid lanes get a digit of their own (256 + lane): no peers
+    const unsigned dig = valid ? (unsigned)((key[i] >> shift) & 0xFF) : 256u + lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, dig);
+    const unsigned rank = __popc(peers & lt);
+    unsigned pos = 0;
+    if (valid) pos = wh[warp][dig] + rank;
+    __syncwarp();
+    if (valid) {
+      key2[pos] = key[i];
+      idx2[pos] = idx[i];
+      if (rank == 0) wh[warp][dig] += __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// atoms[j] = (x, y, z, 0) of the j-th sorted atom (idx: within species).
+__global__ void gather_kernel(const float *__restrict__ xyz, long long n,
+                              const long long *__restrict__ start, int ns,
+                              const unsigned long long *__restrict__ key,
+                              const int *__restrict__ idx,
+                              float4 *__restrict__ atoms) {
+  const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int s = (int)(key[j] >> 32);
+  const long long src = start[s] + idx[j];
+  atoms[j] = make_float4(xyz[src], xyz[n + src], xyz[2 * n + src], 0.f);
+}
+
+// Bounding box of every tile (one warp per tile; tiles {first, count}).
+__global__ void tile_boxes_kernel(const float4 *__restrict__ atoms,
+                                  const int2 *__restrict__ tiles, int ntiles,
+                                  TileBox *__restrict__ boxes) {
+  const int t = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= ntiles) return;
+  const int2 tl = tiles[t];
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int i = lane; i < tl.y; i += 32) {
+    const float4 a = atoms[tl.x + i];
+    const float v[3] = {a.x, a.y, a.z};
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], v[d]);  // NaN skipped, as by the host's std::min
+      hi[d] = fmaxf(hi[d], v[d]);
+    }
+  }
+  for (int d = 0; d < 3; ++d)
+    for (int off = 16; off > 0; off >>= 1) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+    }
+  if (lane == 0) {
+    TileBox b;
+    for (int d = 0; d < 3; ++d) {
+      b.lo[d] = lo[d];
+      b.hi[d] = hi[d];
+    }
+    boxes[t] = b;
+  }
+}
+
+}  // namespace
+
+Error model_upload_sorted(Model *m, const float *x, const float *y, const float *z,
+                          const int64_t *counts, int nspecies, float *pin,
+                          cudaStream_t st) {
+  int64_t natoms = 0;
+  for (int s = 0; s < nspecies; ++s) natoms += counts[s];
+  const long long n = natoms;
+  m->nspecies = nspecies;
+  m->natoms = natoms;
+  std::vector<long long> start(nspecies + 1, 0);
+  std::vector<int> bits(nspecies);
+  for (int s = 0; s < nspecies; ++s) {
+    start[s + 1] = start[s] + counts[s];
+    int b = 4;  // the host's grid: about 2 cells per atom, 16^3 to 1024^3
+    while (b < 10 && (int64_t(1) << (3 * b)) < 2 * counts[s]) ++b;
+    bits[s] = b;
+  }
+  m->tile_start.assign(1, 0);
+  m->tiles.clear();
+  m->boxes.clear();  // on the device; copied to the host when a plan needs them
+  m->sp_start.clear();
+  m->sp_count.clear();
+  for (int s = 0; s < nspecies; ++s) {
+    m->sp_start.push_back(start[s]);
+    m->sp_count.push_back(counts[s]);
+    for (int64_t t0 = 0; t0 < counts[s]; t0 += kTile)
+      m->tiles.push_back(make_int2((int)(start[s] + t0),
+                                   (int)std::min<int64_t>(kTile, counts[s] - t0)));
+    m->tile_start.push_back((int)m->tiles.size());
+  }
+  const int ntiles = (int)m->tiles.size();
+  const size_t abytes = sizeof(float4) * n, tbytes = sizeof(int2) * std::max(ntiles, 1),
+               bbytes = sizeof(TileBox) * std::max(ntiles, 1);
+  // raw coordinates through the pinned staging (3n floats)
+  std::memcpy(pin, x, sizeof(float) * n);
+  std::memcpy(pin + n, y, sizeof(float) * n);
+  std::memcpy(pin + 2 * n, z, sizeof(float) * n);
+  const long long nblk = (n + kSortChunk - 1) / kSortChunk;
+  float *d_xyz = nullptr;
+  unsigned long long *k1 = nullptr, *k2 = nullptr;
+  int *i1 = nullptr, *i2 = nullptr;
+  unsigned *cnt = nullptr, *lohi = nullptr;
+  long long *d_start = nullptr;
+  int *d_bits = nullptr;
+  auto cleanup = [&] {
+    for (void *p : {(void *)d_xyz, (void *)k1, (void *)k2, (void *)i1, (void *)i2,
+                    (void *)cnt, (void *)lohi, (void *)d_start, (void *)d_bits})
+      if (p) cudaFreeAsync(p, st);
+  };
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void **p, size_t b) {
+    if (e == cudaSuccess) e = cudaMallocAsync(p, b, st);
+  };
+  A((void **)&d_xyz, sizeof(float) * 3 * n);
+  A((void **)&k1, 8 * n);
+  A((void **)&k2, 8 * n);
+  A((void **)&i1, 4 * n);
+  A((void **)&i2, 4 * n);
+  A((void **)&cnt, sizeof(unsigned) * kRadix * nblk);
+  A((void **)&lohi, sizeof(unsigned) * 6 * nspecies);
+  A((void **)&d_start, sizeof(long long) * (nspecies + 1));
+  A((void **)&d_bits, sizeof(int) * nspecies);
+  if (e == cudaSuccess && cudaMalloc(&m->d_atoms, abytes) != cudaSuccess) e = cudaErrorMemoryAllocation;
+  if (e == cudaSuccess && cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess) e = cudaErrorMemoryAllocation;
+  if (e == cudaSuccess && cudaMalloc(&m->d_boxes, bbytes) != cudaSuccess) e = cudaErrorMemoryAllocation;
+  if (e != cudaSuccess) {
+    cleanup();
+    return fail(DBX_ERR_NOMEM, "device allocation failed for model");
+  }
+  m->dev_bytes = abytes + tbytes + bbytes;
+  std::vector<unsigned> lohi0(6 * nspecies);
+  for (int s = 0; s < nspecies; ++s)
+    for (int d = 0; d < 3; ++d) {
+      lohi0[s * 6 + d] = 0xFFFFFFFFu;
+      lohi0[s * 6 + 3 + d] = 0u;
+    }
+  e = cudaMemcpyAsync(d_xyz, pin, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(lohi, lohi0.data(), sizeof(unsigned) * lohi0.size(),
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_start, start.data(), sizeof(long long) * start.size(),
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_bits, bits.data(), sizeof(int) * nspecies,
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(m->d_tiles, m->tiles.data(), sizeof(int2) * ntiles,
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    const unsigned g = (unsigned)((n + 255) / 256);
+    bbox_kernel<<<dim3(std::min<unsigned>(g, 64u), nspecies), 256, 0, st>>>(
+        d_xyz, n, d_start, nspecies, lohi);
+    keys_kernel<<<g, 256, 0, st>>>(d_xyz, n, d_start, nspecies, lohi, d_bits, k1, i1);
+    // digits: the code bits, then the species bits (a stable sort by code,
+    // then by species: species-major, code order within, ties in input
+    // order)
+    int code_bits = 0;
+    for (int b : bits) code_bits = std::max(code_bits, 3 * b);
+    int sp_bits = 0;
+    while ((1 << sp_bits) < nspecies) ++sp_bits;
+    std::vector<int> shifts;
+    for (int sh = 0; sh < code_bits; sh += 8) shifts.push_back(sh);
+    for (int sh = 0; sh < sp_bits; sh += 8) shifts.push_back(32 + sh);
+    for (int sh : shifts) {
+      radix_count_kernel<<<(unsigned)nblk, kSortThreads, 0, st>>>(k1, n, sh, cnt);
+      radix_scan_kernel<<<1, 1024, 0, st>>>(cnt, (long long)kRadix * nblk);
+      radix_scatter_kernel<<<(unsigned)nblk, kSortThreads, 0, st>>>(k1, i1, n, sh, cnt,
+                                                                  k2, i2);
+      std::swap(k1, k2);
+      std::swap(i1, i2);
+    }
+    gather_kernel<<<g, 256, 0, st>>>(d_xyz, n, d_start, nspecies, k1, i1, m->d_atoms);
+    tile_boxes_kernel<<<(unsigned)((ntiles * 32LL + 255) / 256), 256, 0, st>>>(
+        m->d_atoms, m->d_tiles, ntiles, m->d_boxes);
+    e = cudaGetLastError();
+  }
+  cleanup();
+  if (e != cudaSuccess) return fail(DBX_ERR_CUDA, std::string("device sort: ") +
+                                                      cudaGetErrorString(e));
+  return ok();
+}
+
+Error model_host_boxes(Model *m, cudaStream_t st) {
+  if (m->boxes.size() == m->tiles.size()) return ok();
+  if (!m->d_boxes) return fail(DBX_ERR_ARG, "model has no tile boxes");
+  m->boxes.resize(m->tiles.size());
+  DBX_CUDA_TRY(cudaMemcpyAsync(m->boxes.data(), m->d_boxes,
+                               sizeof(TileBox) * m->tiles.size(),
+                               cudaMemcpyDeviceToHost, st));
+  DBX_CUDA_TRY(cudaStreamSynchronize(st));
+  return ok();
+}
+
+}  // namespace dbx

@@ -246,3 +246,73 @@ def test_bad_arguments(engine):
     with pytest.raises(cd.DebyeError) as e:
         engine.histogram(stale, 0.1, 10)
     assert e.value.code == -8
+
+
+@pytest.mark.parametrize("rstep", [1e-3, 4e-4])
+def test_device_sort_large_model(engine, orc, rstep):
+    """Models of 32,768 atoms or more are sorted on the device; their
+    histograms (one window, and several windows, whose plan copies the tile
+    boxes back to the host) equal the oracle's."""
+    m = lattice.spinel(radius=34.0, target=40000, seed=19, rstep=rstep)
+    assert m.natoms >= 32768
+    nbins = cd.channels(m.rmax, rstep)
+    h = gpu_vs_oracle(engine, orc, m.xyz, m.counts, rstep, nbins)
+    assert int(h.sum()) == m.pairs
+
+
+DEVICE_SORT_EDGES = r"""
+import numpy as np, re, sys
+sys.path.insert(0, %r)
+import cudebye_gb300 as cd
+from cudebye_gb300 import lattice
+from oracle import pyoracle as orc
+rng = np.random.default_rng(5)
+def check(e, xyz, counts, rstep, nbins):
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    m = e.upload(xyz, counts)
+    try:
+        got = e.histogram(m, rstep, nbins)
+    finally:
+        m.free()
+    want, bad = orc.model_histograms(xyz, counts, rstep, nbins)
+    assert bad == 0
+    np.testing.assert_array_equal(got, want)
+with cd.Engine(0) as e:
+    # empty and one-atom species among others, many species
+    counts = [0, 1, 300, 0, 129, 128, 7, 1000, 2, 0, 55]
+    check(e, rng.uniform(-9, 9, (sum(counts), 3)), counts, 1e-3, cd.channels(32, 1e-3))
+    # every atom at one point (no extent), and a flat layer (one axis flat)
+    check(e, np.zeros((300, 3)), [200, 100], 0.01, 10)
+    flat = rng.uniform(-5, 5, (400, 3)); flat[:, 2] = 1.5
+    check(e, flat, [400], 1e-3, cd.channels(15, 1e-3))
+    # a lattice with exact ties, several windows
+    g = np.arange(10, dtype=np.float32) * np.float32(0.5)
+    lat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    check(e, lat, [600, 400], 2e-5, cd.channels(8, 2e-5))
+    # a NaN coordinate: the engine bins its 50 pairs (49 others and itself)
+    # out of range, a deliberate difference from the reference, whose
+    # (int)roundf(NaN) depends on the platform's conversion
+    xyz = rng.uniform(-3, 3, (50, 3)).astype(np.float32); xyz[7, 1] = np.nan
+    m = e.upload(xyz, [50])
+    try:
+        e.histogram(m, 1e-3, cd.channels(12, 1e-3))
+        raise SystemExit("no range error")
+    except cd.DebyeError as err:
+        got = int(re.search(r"(\d+) distances", str(err)).group(1))
+    finally:
+        m.free()
+    assert got == 50, got
+print("OK")
+"""
+
+
+def test_device_sort_edge_cases():
+    """The device sort forced for every model size: empty, one-atom and
+    many species, coincident atoms, a flat layer and exact lattice ties over
+    several windows give the oracle's histograms; a NaN coordinate gives an
+    exact range-error count."""
+    code = DEVICE_SORT_EDGES % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, DBX_DEVICE_SORT_MIN="1")
+    r = subprocess.run(["python", "-c", code], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
