@@ -388,13 +388,17 @@ def io_bench(eng, nfiles=16, seed=8):
     return out
 
 
-def serving_bench(rates=(5, 20, 50, 100, 200), seconds=6.0, pool=32, seed=4):
+def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, pool=32,
+                  seed=4, budget_gib=16):
     """The serving form: Poisson arrivals at each rate for `seconds`; each
     request is a spherical lattice model of 1,000-200,000 atoms
     (log-uniform, 1-4 species) with its own 2theta grid of 2,000-20,000
     points, or, with probability 0.2, a re-scoring of a resident model with
     new B factors. Latency = submit to result, measured by the server.
-    Requests are drawn from a pool of `pool` seeded models (generated once)."""
+    Requests are drawn from a pool of `pool` seeded models (generated once).
+    The server admits by HBM footprint within `budget_gib`, evicting idle
+    resident models; a re-score of a model evicted meanwhile fails with
+    DBX_ERR_MODEL and is counted, not timed."""
     import concurrent.futures as cf
     import cudebye_gb300 as cd
     from cudebye_gb300 import lattice
@@ -402,18 +406,23 @@ def serving_bench(rates=(5, 20, 50, 100, 200), seconds=6.0, pool=32, seed=4):
     models = [lattice.serving_request(rng) for _ in range(pool)]
     grids = [m.k_grid()[1] for m in models]
     out = []
-    with cd.Server(0) as srv:
+    with cd.Server(0, hbm_budget=budget_gib << 30) as srv:
         # warm-up: one pass over a few pool models
         for m, K in list(zip(models, grids))[:4]:
             srv.wait(srv.submit(m.species, m.rstep, m.nbins, K, xyz=m.xyz,
                                 counts=m.counts), len(K))
         for rate in rates:
-            lat, done_t, resident = [], [], []
+            lat, done_t, resident, failed = [], [], [], []
             lock = threading.Lock()
             ex = cf.ThreadPoolExecutor(max_workers=64)
 
             def waiter(t, nq, pi, t0):
-                I, mid, ms = srv.wait(t, nq)
+                try:
+                    I, mid, ms = srv.wait(t, nq)
+                except cd.DebyeError as err:  # re-score of an evicted model
+                    with lock:
+                        failed.append(err.code)
+                    return
                 with lock:
                     lat.append(ms)
                     done_t.append(time.perf_counter() - t0)
@@ -452,6 +461,7 @@ def serving_bench(rates=(5, 20, 50, 100, 200), seconds=6.0, pool=32, seed=4):
             ex.shutdown()
             span = max(done_t) if done_t else seconds
             out.append({"rate": rate, "submitted": nsub, "rescored": nres,
+                        "failed_evicted": len(failed),
                         "patterns_per_s": len(lat) / span,
                         "p50_ms": float(np.percentile(lat, 50)),
                         "p99_ms": float(np.percentile(lat, 99))})
@@ -460,6 +470,7 @@ def serving_bench(rates=(5, 20, 50, 100, 200), seconds=6.0, pool=32, seed=4):
                if o["patterns_per_s"] >= 0.9 * o["rate"]] or [0])
     return {"rates": out, "saturation_req_per_s": sat,
             "seconds_per_rate": seconds, "pool_models": pool,
+            "hbm_budget_gib": budget_gib,
             "rounds": st["rounds"], "evictions": st["evictions"],
             "timing": "host clock; latency measured by the server from "
                       "submit to result (incl. upload, queueing, readback)"}

@@ -149,6 +149,9 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
                           cudaStream_t stream);
 Error model_host_boxes(Model *m, cudaStream_t stream);
 void model_release(Model *m);
+// The same, device arrays freed in `stream` order (no device-wide wait);
+// for a model no queued or running work uses.
+void model_release_async(Model *m, cudaStream_t stream);
 
 inline int npairs_of(int p) { return p * (p + 1) / 2; }
 inline int pair_index(int p, int row, int col) {

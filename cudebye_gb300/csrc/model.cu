@@ -240,6 +240,17 @@ size_t model_device_bytes(const Model &m) {
   return m.dev_bytes + m.hist_bytes + m.plan_bytes;
 }
 
+void model_release_async(Model *m, cudaStream_t stream) {
+  for (void *p : {(void *)m->d_atoms, (void *)m->d_tiles, (void *)m->d_boxes,
+                  (void *)m->d_hist})
+    if (p) cudaFreeAsync(p, stream);
+  m->d_atoms = nullptr;
+  m->d_tiles = nullptr;
+  m->d_boxes = nullptr;
+  m->d_hist = nullptr;
+  model_release(m);  // the plan cache, if any
+}
+
 void model_release(Model *m) {
   if (m->d_atoms) cudaFree(m->d_atoms);
   if (m->d_tiles) cudaFree(m->d_tiles);

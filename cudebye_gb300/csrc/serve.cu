@@ -33,6 +33,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -165,16 +166,17 @@ void complete(dbx_server *s, Req *r, int status, const std::string &msg) {
 // `need` more bytes fit. Worker thread, lock held.
 bool make_room(dbx_server *s, size_t need) {
   if (!s->budget) return true;
+  if (s->used + need + s->lane_reserve <= s->budget) return true;
+  std::set<int64_t> named;  // models a queued request refers to
+  for (Req *q : s->queue)
+    if (q->model) named.insert(q->model);
   while (s->used + need + s->lane_reserve > s->budget) {
     int64_t victim = 0;
     double oldest = 1e300;
     for (auto &kv : s->models) {
       const SModel &sm = kv.second;
-      if (!sm.ready || sm.busy) continue;
-      bool named = false;
-      for (Req *q : s->queue)
-        if (q->model == kv.first) named = true;
-      if (!named && sm.last_use < oldest) {
+      if (!sm.ready || sm.busy || named.count(kv.first)) continue;
+      if (sm.last_use < oldest) {
         oldest = sm.last_use;
         victim = kv.first;
       }
@@ -182,8 +184,12 @@ bool make_room(dbx_server *s, size_t need) {
     if (!victim) return false;
     SModel &sm = s->models[victim];
     s->used -= sm.bytes();
-    model_release(sm.m.get());
-    release(&sm.S);
+    // idle: no round in flight uses it; freed in stream order, without the
+    // device-wide wait of cudaFree
+    model_release_async(sm.m.get(), s->lanes[0].stream);
+    if (sm.S.p) cudaFreeAsync(sm.S.p, s->lanes[0].stream);
+    sm.S.p = nullptr;
+    sm.S.bytes = 0;
     s->models.erase(victim);
     ++s->evicted;
   }
