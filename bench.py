@@ -209,16 +209,16 @@ def cpu_baseline(m, K, budget_s=12.0, threads=0):
     }
 
 
-def batch_bench(eng, steps=5, seed=3, nmodels=256, check=8, plain_models=None):
+def batch_bench(eng, steps=5, seed=3, nmodels=256, plain_models=None):
     """The batched form: 256 independent models (sc / fcc / spinel-like,
     N log-uniform 2k-60k, 1-4 species, sigma U[0.03,0.1], B U[0.2,1.5]) on
     the 6,001-point q grid. Patterns/s of (a) the batched engine (one
     histogram launch + one tensor-core contraction for all 256 models,
     CUDA-graph replay) and (b) the plain unbatched FP32 GPU form (model by
     model: one-thread-per-pair global-atomic histogram + FP32 direct Debye
-    sum). Max relative error of (a) against the FP64 direct sum on `check`
-    sampled models (every 10th q): the reference's arithmetic on the
-    device, which the tests hold within 1e-11 of the CPU FP64 oracle."""
+    sum). Max relative error of every pattern of (a) against the FP64
+    direct sum (every 10th q): the reference's arithmetic on the device,
+    which the tests hold within 1e-11 of the CPU FP64 oracle."""
     from cudebye_gb300 import lattice
     mods = lattice.batch256(seed=seed, nmodels=nmodels)
     tt, K = mods[0].k_grid()
@@ -235,15 +235,14 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, check=8, plain_models=None):
             I = eng.patterns(hs, 1e-3, nb, sp, K)
             ts.append(time.perf_counter() - t0)
         t_tc = float(np.median(ts))
-        rng = np.random.default_rng(seed)
-        pick = sorted(rng.choice(len(mods), size=min(check, len(mods)),
-                                 replace=False).tolist())
-        worst = 0.0
-        for i in pick:  # histograms resident from the pass
+        # every pattern's max relative error at every 10th q against the
+        # FP64 direct sum of its resident histograms
+        per = []
+        for i in range(len(mods)):
             want = eng.intensity(hs[i], 1e-3, nb[i], mods[i].species,
                                  K[::10], mode="fp64")
-            worst = max(worst, float(np.max(np.abs(I[i, ::10] - want)
-                                            / np.abs(want))))
+            per.append(float(np.max(np.abs(I[i, ::10] - want) / np.abs(want))))
+        worst = max(per)
         # plain form over a subset (it is slow), scaled per pattern
         sub = list(range(len(mods))) if plain_models is None else \
             list(range(min(plain_models, len(mods))))
@@ -262,8 +261,12 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, check=8, plain_models=None):
         "patterns_per_s_plain": len(mods) / t_plain,
         "speedup_batched_vs_plain": t_plain / t_tc,
         "ms_per_batch": t_tc * 1e3,
-        "max_rel_err_vs_fp64": worst, "err_models_checked": len(pick),
-        "err_reference": "FP64 direct sum on the device (every 10th q)",
+        "max_rel_err_vs_fp64": worst, "err_models_checked": len(per),
+        "median_pattern_max_rel_err": float(np.median(per)),
+        "patterns_over_1e-6": int(sum(e > 1e-6 for e in per)),
+        "err_reference": "FP64 direct sum on the device (every 10th q), the "
+                         "reference's arithmetic; tests hold it within 1e-11 "
+                         "of the CPU FP64 oracle",
         "timing": "host wall clock around dbx_patterns (H2D species/K, graph "
                   "replay, D2H of all intensities), median of %d passes" % steps,
     }
