@@ -453,6 +453,12 @@ __global__ void __launch_bounds__(kPThreads, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t sA = base + st * kPStageBytes, sB = sA + kASlabBytes;
+        // descriptors of the stage's first core matrices; the others differ
+        // in the start-address field only (16-byte units, no carry out of
+        // the field: shared addresses are below 256 KB), so each MMA needs
+        // one add per operand instead of a descriptor build (the single
+        // issuing thread limited the MMA rate)
+        const uint64_t adb = make_desc(sA, 128, 1024), bdb = make_desc(sB, 128, 1024);
 #pragma unroll
         for (int w = 0; w < NCLS; ++w) {
 #pragma unroll
@@ -460,8 +466,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
             const int u = w - s;
 #pragma unroll
             for (int kk = 0; kk < kKS / 16; ++kk) {
-              const uint64_t ad = make_desc(sA + s * kABlock * 2 + kk * 256, 128, 1024);
-              const uint64_t bd = make_desc(sB + u * kBBlock * 2 + kk * 256, 128, 1024);
+              const uint64_t ad = adb + (uint64_t)((s * kABlock * 2 + kk * 256) >> 4);
+              const uint64_t bd = bdb + (uint64_t)((u * kBBlock * 2 + kk * 256) >> 4);
               const uint32_t acc = (ks > 0 || s > 0 || kk > 0) ? 1u : 0u;
               mma_bf16(acc_base + w * kTN, ad, bd, idesc, acc);
             }
