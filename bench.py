@@ -503,7 +503,8 @@ def run_reference(args):
         "config": {"workload": m.label, "atoms": m.natoms,
                    "species": len(m.counts), "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
                    "bins": m.nbins, "rstep": m.rstep, "q_points": len(K),
-                   "binned_pairs": m.pairs, "parallelism": "replicas",
+                   "binned_pairs": m.pairs,
+                   "parallelism": "host threads of rank 0",
                    "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": v, "unit": METRIC, "cores": b["cores"],
                          "kind": "port", "sample": b["sample"]},
