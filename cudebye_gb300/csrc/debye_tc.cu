@@ -89,42 +89,75 @@ __device__ inline long long fixed31(double v) {
   return r > 2147483647LL ? 2147483647LL : (r < -2147483647LL ? -2147483647LL : r);
 }
 
+// The basis and twiddle angles advance by a fixed step (dr or L dr per
+// element), so each thread evaluates sincos (FP64, slow on this part) at
+// the first of a run of kRun elements and at the step, and advances by
+// rotation (two FP64 products and an FMA per component); the rotations
+// add a few ulp over a run, far below the 2^-31 fixed-point resolution of
+// the basis and the double-float twiddles' 2^-48.
+constexpr int kRun = 16;
+
 // Basis digits: rows [0,Qp) cos(K_q j dr), rows [Qp,2Qp) sin(K_q j dr).
-// Layout: [row tile][slab][digit][tiled 128 x 64].
+// Layout: [row tile][slab][digit][tiled 128 x 64]. One thread per row and
+// run of kRun columns; eight columns of a digit are one 16-byte store.
 __global__ void basis_kernel(const double *__restrict__ K, int nq, int Qp,
                              double rstep, __nv_bfloat16 *__restrict__ A) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= 2LL * Qp * kL) return;
-  const int j = (int)(idx % kL);
-  const int m = (int)(idx / kL);
+  if (idx >= 2LL * Qp * (kL / kRun)) return;
+  const int m = (int)(idx % (2 * Qp));
+  const int j0 = (int)(idx / (2 * Qp)) * kRun;
   const bool sinrow = m >= Qp;
   const int q = sinrow ? m - Qp : m;
-  double v = 0.0;
+  double s = 0.0, c = 0.0, ss = 0.0, cs = 1.0;
   if (q < nq) {
-    const double ph = K[q] * ((double)j * rstep);
-    v = sinrow ? sin(ph) : cos(ph);
+    sincos(K[q] * ((double)j0 * rstep), &s, &c);
+    sincos(K[q] * rstep, &ss, &cs);
   }
-  float d[4];
-  split4(fixed31(v), d);
-  const int mt = m / kTM, row = m % kTM, ks = j / kKS, k = j % kKS;
-  const size_t base = (size_t)(mt * kNSlab + ks) * kND * kABlock;
+  const int mt = m / kTM, row = m % kTM;
 #pragma unroll
-  for (int s = 0; s < kND; ++s)
-    A[base + (size_t)s * kABlock + tiled_off(row, k)] = __float2bfloat16_rn(d[s]);
+  for (int g = 0; g < kRun; g += 8) {
+    alignas(16) __nv_bfloat16 dig[kND][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float d[4];
+      split4(fixed31(sinrow ? s : c), d);
+#pragma unroll
+      for (int t = 0; t < kND; ++t) dig[t][i] = __float2bfloat16_rn(d[t]);
+      const double s2 = fma(s, cs, c * ss), c2 = fma(c, cs, -(s * ss));
+      s = s2;
+      c = c2;
+    }
+    const int j = j0 + g, ks = j / kKS, k = j % kKS;
+    const size_t base = (size_t)(mt * kNSlab + ks) * kND * kABlock + tiled_off(row, k);
+#pragma unroll
+    for (int t = 0; t < kND; ++t)
+      *reinterpret_cast<uint4 *>(A + base + (size_t)t * kABlock) =
+          *reinterpret_cast<const uint4 *>(dig[t]);
+  }
 }
 
 // Twiddles per (chunk, q): alpha = K_q * ch*L*dr; (sin hi, sin lo, cos hi,
-// cos lo) as double-floats.
+// cos lo) as double-floats. One thread per q and run of kRun chunks.
 __global__ void twiddle_kernel(const double *__restrict__ K, int nq, int Qp,
                                int nch, double rstep, float4 *__restrict__ tw) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)nch * Qp) return;
+  if (idx >= (long long)(nch / kRun) * Qp) return;
   const int q = (int)(idx % Qp);
-  const int ch = (int)(idx / Qp);
-  double s = 0.0, c = 1.0;
-  if (q < nq) sincos(K[q] * ((double)ch * kL * rstep), &s, &c);
-  const float sh = (float)s, ch_ = (float)c;
-  tw[idx] = make_float4(sh, (float)(s - (double)sh), ch_, (float)(c - (double)ch_));
+  const int ch0 = (int)(idx / Qp) * kRun;
+  double s = 0.0, c = 1.0, ss = 0.0, cs = 1.0;
+  if (q < nq) {
+    sincos(K[q] * ((double)ch0 * kL * rstep), &s, &c);
+    sincos(K[q] * ((double)kL * rstep), &ss, &cs);
+  }
+#pragma unroll 4
+  for (int i = 0; i < kRun; ++i) {
+    const float sh = (float)s, ch_ = (float)c;
+    tw[(size_t)(ch0 + i) * Qp + q] =
+        make_float4(sh, (float)(s - (double)sh), ch_, (float)(c - (double)ch_));
+    const double s2 = fma(s, cs, c * ss), c2 = fma(c, cs, -(s * ss));
+    s = s2;
+    c = c2;
+  }
 }
 
 // Chunk weights as digits, one warp per (tile, column). The weight of bin
@@ -635,10 +668,10 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
   if (!same_grid) {
     DBX_TRY(buf_grow(&st->basis, (size_t)nrt * kNSlab * kASlabBytes, delta, as));
     DBX_TRY(buf_grow(&st->twid, sizeof(float4) * (size_t)nch_cap * Qp, delta, as));
-    const long long nb = 2LL * Qp * kL;
+    const long long nb = 2LL * Qp * (kL / kRun);
     basis_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, stream>>>(
         d_K, nq, Qp, rstep, (__nv_bfloat16 *)st->basis.p);
-    const long long nt2 = (long long)nch_cap * Qp;
+    const long long nt2 = (long long)(nch_cap / kRun) * Qp;  // nch_cap: multiple of 64
     twiddle_kernel<<<(unsigned)((nt2 + 255) / 256), 256, 0, stream>>>(
         d_K, nq, Qp, nch_cap, rstep, (float4 *)st->twid.p);
     DBX_CUDA_TRY(cudaGetLastError());
