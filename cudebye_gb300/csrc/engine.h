@@ -173,6 +173,11 @@ struct HistSeg {  // one (model, pair, bin window) accumulated in smem
   // item index = task-local position.
   int shape;
   int ti0, tni, tj0, tnj;
+  // Bins of the window this segment counts, window-relative: [own_lo,
+  // own_lo + own_len); the whole window (0, wl) unless overlapping windows
+  // of a histogram share bins. own_lo is even, and own_lo + own_len is even
+  // or the window's end.
+  int own_lo, own_len;
 };
 constexpr int kSegList = 0, kSegRect = 1, kSegTri = 2;
 struct HistTask {  // one CTA-sized slice of a segment's tile pairs

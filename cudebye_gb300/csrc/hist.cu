@@ -200,6 +200,15 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     const unsigned nbins = sg.nbins;
     const unsigned base = 0x4B000000u + kb;
     const bool full_window = kb == 0 && wl >= nbins;
+    // The pairs this segment counts are its window's bins [own_lo, own_lo +
+    // own_len) (the whole window unless overlapping windows share bins):
+    // the pair loop sees that range as its window, by offsetting the base,
+    // the histogram pointer and the spare counters' virtual bins (own_lo is
+    // even, so bins keep their parity; the raw-bit addresses are unchanged).
+    const unsigned olo = (unsigned)sg.own_lo;
+    const unsigned pbase = base + olo, pwl = (unsigned)sg.own_len, pkb = kb + olo;
+    unsigned long long *pgh = gh + olo;
+    const unsigned pvo = vo - olo, pvi = vi - olo, pvend = vend - olo;
     for (int it_i = tk.item_begin + warp; it_i < tk.item_end;
          it_i += kHistThreads / 32) {
       const int2 it = seg_item(sg, items, it_i);
@@ -223,18 +232,18 @@ __global__ void __launch_bounds__(kHistThreads, 1)
       const bool all_valid = !diag && TI.y == kTile;  // warp-uniform
       if (all_valid) {
         if (full_window)
-          pair_loop<true, true>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
-                                nbins, gh, vo, vi, vend, oor_total);
+          pair_loop<true, true>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+                                nbins, pgh, pvo, pvi, pvend, oor_total);
         else
-          pair_loop<true, false>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
-                                 nbins, gh, vo, vi, vend, oor_total);
+          pair_loop<true, false>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+                                 nbins, pgh, pvo, pvi, pvend, oor_total);
       } else {
         if (full_window)
-          pair_loop<false, true>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
-                                 nbins, gh, vo, vi, vend, oor_total);
+          pair_loop<false, true>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+                                 nbins, pgh, pvo, pvi, pvend, oor_total);
         else
-          pair_loop<false, false>(bj, TJ.y, x, y, z, jlim, inv, base, sadj, wl, kb,
-                                  nbins, gh, vo, vi, vend, oor_total);
+          pair_loop<false, false>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+                                  nbins, pgh, pvo, pvi, pvend, oor_total);
       }
     }
     __syncthreads();
@@ -251,10 +260,11 @@ __global__ void __launch_bounds__(kHistThreads, 1)
   }
 }
 
-// Sum the packed windows of each segment's tasks into the int64 histogram.
-// A segment owns its window's bins (windows of one pair do not overlap), so
-// the adds are plain read-modify-writes; the wrap corrections of the tile
-// kernel were made earlier on the same stream.
+// Sum the packed windows of each segment's tasks into the int64 histogram
+// (bins a segment does not count hold 0 there). A histogram of one window
+// has one segment owning every bin: plain read-modify-writes; the windows of
+// a wider histogram overlap, so their sums are atomic. The wrap corrections
+// of the tile kernel were made earlier on the same stream.
 __global__ void hist_reduce_kernel(const unsigned *__restrict__ partial,
                                    int words_per_task,
                                    const HistSeg *__restrict__ segs) {
@@ -269,8 +279,13 @@ __global__ void hist_reduce_kernel(const unsigned *__restrict__ partial,
       hi += w >> 16;
     }
     unsigned long long *g = sg.out + sg.kb + 2 * i;
-    g[0] += lo;
-    if (2 * i + 1 < sg.wl) g[1] += hi;  // bin wl (odd wl) counts range errors
+    if (sg.kb == 0 && (unsigned)sg.wl >= sg.nbins) {  // one window: sole owner
+      g[0] += lo;
+      if (2 * i + 1 < sg.wl) g[1] += hi;  // bin wl (odd wl) counts range errors
+    } else {  // windows of one histogram may overlap
+      if (lo) atomicAdd(&g[0], lo);
+      if (hi && 2 * i + 1 < sg.wl) atomicAdd(&g[1], hi);
+    }
   }
 }
 
@@ -375,6 +390,12 @@ static void box_bins(const TileBox &A, const TileBox &B, double inv,
     dmax2 += h * h;
   }
   // FP32 distances carry a relative error of a few 1e-7; widen generously.
+  // A box with a NaN or infinite coordinate may reach any bin (and beyond).
+  if (!std::isfinite(dmax2) || !std::isfinite(dmin2)) {
+    *kmin = 0;
+    *kmax = INT64_MAX;
+    return;
+  }
   *kmin = (int64_t)std::floor(std::sqrt(dmin2) * inv * (1 - 1e-5)) - 2;
   *kmax = (int64_t)std::ceil(std::sqrt(dmax2) * inv * (1 + 1e-5)) + 2;
 }
@@ -449,6 +470,8 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
         s.task_begin = s.task_end = 0;
         s.nbins = (unsigned)nbins;
         s.shape = (a == b) ? kSegTri : kSegRect;
+        s.own_lo = 0;
+        s.own_len = s.wl;
         s.ti0 = I0;
         s.tni = nI;
         s.tj0 = J0;
@@ -485,12 +508,97 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
         while (k < nth && acc * nth >= nitems * k) row_cut[k++] = I + 1;
       }
     }
+    // Window geometry. Disjoint: window w covers [w W, (w + 1) W). Or
+    // overlapping where nbins < nwin W: window w starts at an even kbw[w],
+    // evenly spaced, the last ending at nbins. Window w owns the bins
+    // [own[w], own[w + 1]) (boundaries even, inside both neighbours). A tile
+    // pair whose bin range lies inside one window is listed there alone and
+    // counts all its pairs in it ("whole" list); any other is listed in
+    // every window whose owned bins its range reaches and counts only
+    // those ("owned" list). Overlap saves the second pass of tile pairs
+    // that straddle a boundary when windows are wide against the tile
+    // pairs' ranges (a histogram slightly wider than one window), and costs
+    // narrower owned ranges when they are not (fine bins): each species
+    // pair takes the geometry under which evenly spaced sample tile pairs
+    // list fewer pairs.
+    struct Geom {
+      std::vector<int64_t> kbw, wlw, own;
+    };
+    auto make_geom = [&](bool overlap) {
+      Geom g;
+      g.kbw.resize(nwin);
+      g.wlw.resize(nwin);
+      g.own.resize(nwin + 1);
+      const int64_t last = std::max<int64_t>(0, (nbins - W + 1) & ~int64_t(1));
+      for (int64_t w = 0; w < nwin; ++w) {
+        g.kbw[w] = overlap ? ((w * last) / (nwin - 1)) & ~int64_t(1) : w * W;
+        g.wlw[w] = std::min<int64_t>(W, nbins - g.kbw[w]);
+      }
+      g.own[0] = 0;
+      g.own[nwin] = nbins;
+      for (int64_t w = 1; w < nwin; ++w)  // middle of the overlap, even
+        g.own[w] = overlap ? ((g.kbw[w] + g.kbw[w - 1] + g.wlw[w - 1]) / 2) & ~int64_t(1)
+                           : g.kbw[w];
+      return g;
+    };
+    // Lists of a tile pair with bin range [kmin, kmax]: emit(2 w) for the
+    // whole list of window w, emit(2 w + 1) for its owned list.
+    auto assign = [&](const Geom &g, int64_t kmin, int64_t kmax, auto &&emit) {
+      kmin = std::max<int64_t>(kmin, 0);
+      if (kmin >= nbins) {  // entirely beyond rmax: the last window reports
+        emit(2 * (nwin - 1));  // them as range errors
+        return;
+      }
+      // the last window starting at or below kmin, and the one before
+      const int64_t wc = std::upper_bound(g.kbw.begin(), g.kbw.end(), kmin) - g.kbw.begin() - 1;
+      int64_t whole = -1;
+      for (int64_t w = std::max<int64_t>(0, wc - 1); w <= wc; ++w)
+        if (g.kbw[w] <= kmin &&  // the last window counts bins >= nbins too
+            (w == nwin - 1 || kmax < g.kbw[w] + g.wlw[w]))
+          whole = w;
+      if (whole >= 0) {
+        emit(2 * whole);
+        return;
+      }
+      const int64_t hi = std::min<int64_t>(kmax, nbins - 1);
+      const int64_t w0 = std::upper_bound(g.own.begin(), g.own.end(), kmin) - g.own.begin() - 1;
+      const int64_t w1 = std::upper_bound(g.own.begin(), g.own.end(), hi) - g.own.begin() - 1;
+      for (int64_t w = w0; w <= std::min(w1, nwin - 1); ++w) emit(2 * w + 1);
+    };
+    const Geom gd = make_geom(false), go = make_geom(true);
+    bool overlap = false;
+    {
+      double cd = 0, co = 0;
+      const int nI = I1 - I0;
+      for (int smp = 0; smp < 4096 && nI > 0; ++smp) {
+        const int I = I0 + (int)((int64_t)smp * nI / 4096);
+        const int Jlo = (a == b) ? I : Jb0;
+        const int J = Jlo + (int)(((int64_t)smp * 7919) % std::max(1, Jb1 - Jlo));
+        int64_t kmin, kmax;
+        box_bins(m.boxes[I], m.boxes[J], inv, &kmin, &kmax);
+        const double np = (double)item_pairs(m.tiles[I].y, m.tiles[J].y, a == b && I == J);
+        assign(gd, kmin, kmax, [&](int64_t) { cd += np; });
+        assign(go, kmin, kmax, [&](int64_t) { co += np; });
+      }
+      overlap = co < cd;
+    }
+    const Geom &g = overlap ? go : gd;
+    const std::vector<int64_t> &kbw = g.kbw, &wlw = g.wlw, &own = g.own;
+    for (int64_t w = 1; w < nwin; ++w)
+      if (own[w] < kbw[w] || own[w] > kbw[w - 1] + wlw[w - 1] || own[w] <= own[w - 1])
+        return fail(DBX_ERR_ARG, "internal: histogram windows do not tile the bins");
+    const int64_t nl = 2 * nwin;
     std::vector<WinLists> part(nth);
     auto list_rows = [&](int t) {
       WinLists &L = part[t];
-      L.items.assign(nwin, {});
-      L.pairs.assign(nwin, {});
-      L.sum.assign(nwin, 0);
+      L.items.assign(nl, {});
+      L.pairs.assign(nl, {});
+      L.sum.assign(nl, 0);
+      auto put = [&](int64_t l, int2 it, int np) {
+        L.items[l].push_back(it);
+        L.pairs[l].push_back(np);
+        L.sum[l] += np;
+      };
       for (int I = row_cut[t]; I < row_cut[t + 1]; ++I) {
         const int2 TI = m.tiles[I];
         for (int J = (a == b) ? I : Jb0; J < Jb1; ++J) {
@@ -499,15 +607,7 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
           const int np = (int)item_pairs(TI.y, m.tiles[J].y, diag);
           int64_t kmin, kmax;
           box_bins(m.boxes[I], m.boxes[J], inv, &kmin, &kmax);
-          int64_t w0 = std::max<int64_t>(0, kmin) / W;
-          int64_t w1 = std::min<int64_t>(std::max<int64_t>(kmax, 0), nbins - 1) / W;
-          w0 = std::min(w0, nwin - 1);  // entirely beyond rmax: still run it
-          w1 = std::max(w1, w0);        // so the kernel reports the range error
-          for (int64_t w = w0; w <= w1; ++w) {
-            L.items[w].push_back(it);
-            L.pairs[w].push_back(np);
-            L.sum[w] += np;
-          }
+          assign(g, kmin, kmax, [&](int64_t l) { put(l, it, np); });
         }
       }
     };
@@ -519,15 +619,15 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       list_rows(0);
       for (std::thread &x : th) x.join();
     }
-    // Final positions of every (window, thread) list, then one resize of
-    // the plan's arrays and a parallel copy into place.
-    std::vector<int64_t> off((size_t)nwin * nth);
+    // Final positions of every (list, thread) part, then one resize of the
+    // plan's arrays and a parallel copy into place.
+    std::vector<int64_t> off((size_t)nl * nth);
     size_t at = plan->items.size();
     const size_t first_all = at;
-    for (int64_t w = 0; w < nwin; ++w)
+    for (int64_t l = 0; l < nl; ++l)
       for (int t = 0; t < nth; ++t) {
-        off[(size_t)w * nth + t] = (int64_t)at;
-        at += part[t].items[w].size();
+        off[(size_t)l * nth + t] = (int64_t)at;
+        at += part[t].items[l].size();
       }
     if (at > plan->items.capacity()) {  // grow geometrically across calls
       plan->items.reserve(std::max(at, 2 * plan->items.capacity()));
@@ -537,10 +637,10 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
     plan->item_pairs.resize(at);
     auto place = [&](int t) {
       const WinLists &L = part[t];
-      for (int64_t w = 0; w < nwin; ++w) {
-        const size_t o = (size_t)off[(size_t)w * nth + t];
-        std::copy(L.items[w].begin(), L.items[w].end(), plan->items.begin() + o);
-        std::copy(L.pairs[w].begin(), L.pairs[w].end(), plan->item_pairs.begin() + o);
+      for (int64_t l = 0; l < nl; ++l) {
+        const size_t o = (size_t)off[(size_t)l * nth + t];
+        std::copy(L.items[l].begin(), L.items[l].end(), plan->items.begin() + o);
+        std::copy(L.pairs[l].begin(), L.pairs[l].end(), plan->item_pairs.begin() + o);
       }
     };
     if (nth == 1) {
@@ -552,26 +652,29 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       for (std::thread &x : th) x.join();
     }
     size_t cur = first_all;
-    for (int64_t w = 0; w < nwin; ++w) {
+    for (int64_t l = 0; l < nl; ++l) {
+      const int64_t w = l / 2;
+      const bool owned = l & 1;
       int64_t sp = 0;
       size_t cnt = 0;
       for (const WinLists &L : part) {
-        cnt += L.items[w].size();
-        sp += L.sum[w];
+        cnt += L.items[l].size();
+        sp += L.sum[l];
       }
       if (cnt == 0) continue;
       HistSeg s;
       s.atoms = m.d_atoms;
       s.tiles = m.d_tiles;
       s.out = row;
-      s.kb = (int)(w * W);
-      s.wl = (int)std::min<int64_t>(W, nbins - w * W);
+      s.kb = (int)kbw[w];
+      s.wl = (int)wlw[w];
       s.task_begin = s.task_end = 0;
-      // a tile pair listed in several windows has its out-of-range pairs
-      // counted by the last window only: the others get an unreachable
-      // bound (no distance bins at or beyond 2^32 - 1 in the test)
+      // out-of-range pairs are counted by the last window only: the others
+      // get an unreachable bound (no bin reaches 2^32 - 1 in the test)
       s.nbins = w == nwin - 1 ? (unsigned)nbins : 0xFFFFFFFFu;
       s.shape = kSegList;
+      s.own_lo = owned ? (int)(own[w] - kbw[w]) : 0;
+      s.own_len = owned ? (int)(own[w + 1] - own[w]) : s.wl;
       s.ti0 = s.tni = s.tj0 = s.tnj = 0;
       plan->segs.push_back(s);
       plan->seg_items.push_back(make_int2((int)cur, (int)(cur + cnt)));

@@ -84,14 +84,18 @@ static void sort_species(const float *const xyz[3], int64_t start, int64_t n,
       bx.lo[d] = INFINITY;
       bx.hi[d] = -INFINITY;
     }
+    bool nan = false;
     for (int i = 0; i < cnt; ++i) {
       const float4 a = atoms[start + t0 + i];
       const float v[3] = {a.x, a.y, a.z};
       for (int d = 0; d < 3; ++d) {
+        nan |= v[d] != v[d];
         bx.lo[d] = std::min(bx.lo[d], v[d]);
         bx.hi[d] = std::max(bx.hi[d], v[d]);
       }
     }
+    if (nan)  // a NaN atom's distances are unknown: the box says so
+      for (int d = 0; d < 3; ++d) bx.lo[d] = bx.hi[d] = NAN;
     boxes->push_back(bx);
   }
 }

@@ -228,24 +228,27 @@ __global__ void tile_boxes_kernel(const float4 *__restrict__ atoms,
   if (t >= ntiles) return;
   const int2 tl = tiles[t];
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  bool nan = false;
   for (int i = lane; i < tl.y; i += 32) {
     const float4 a = atoms[tl.x + i];
     const float v[3] = {a.x, a.y, a.z};
     for (int d = 0; d < 3; ++d) {
-      lo[d] = fminf(lo[d], v[d]);  // NaN skipped, as by the host's std::min
+      nan |= v[d] != v[d];
+      lo[d] = fminf(lo[d], v[d]);
       hi[d] = fmaxf(hi[d], v[d]);
     }
   }
+  nan = __any_sync(0xffffffffu, nan);
   for (int d = 0; d < 3; ++d)
     for (int off = 16; off > 0; off >>= 1) {
       lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
       hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
     }
   if (lane == 0) {
-    TileBox b;
+    TileBox b;  // a tile with a NaN atom gets a NaN box, as on the host
     for (int d = 0; d < 3; ++d) {
-      b.lo[d] = lo[d];
-      b.hi[d] = hi[d];
+      b.lo[d] = nan ? NAN : lo[d];
+      b.hi[d] = nan ? NAN : hi[d];
     }
     boxes[t] = b;
   }

@@ -302,6 +302,16 @@ with cd.Engine(0) as e:
     finally:
         m.free()
     assert got == 50, got
+    # the same over several windows: each of the 50 counted once
+    m = e.upload(xyz, [50])
+    try:
+        e.histogram(m, 1e-5, cd.channels(12, 1e-5))
+        raise SystemExit("no range error")
+    except cd.DebyeError as err:
+        got = int(re.search(r"(\d+) distances", str(err)).group(1))
+    finally:
+        m.free()
+    assert got == 50, got
 print("OK")
 """
 
