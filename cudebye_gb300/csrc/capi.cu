@@ -56,6 +56,11 @@ struct dbx_ctx {
   int64_t h2d = 0, d2h = 0;           // bytes copied (dbx_get_traffic)
   std::map<int64_t, std::unique_ptr<dbx::Model>> models;
   int64_t next_id = 1;
+  // Pinned staging of the host-to-device copies made while a call queues
+  // its work (a copy from pageable memory would make the host wait for the
+  // histogram just launched); reset at the start of the calls that use it,
+  // all of which end synchronised.
+  dbx::PinArena arena;
   dbx::HistWorkspace hws;
   dbx::TcState tc;
   dbx::DevBuf tmp_hist, K, ff, I;
@@ -135,7 +140,10 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   size_t delta = 0;
   if (!m->plan_cache || m->plan_rstep != rstep || m->plan_nbins != nbins ||
       m->plan_out != m->d_hist) {
-    if (!m->plan_cache) m->plan_cache = new dbx::HistPlanCache();
+    if (!m->plan_cache) {
+      m->plan_cache = new dbx::HistPlanCache();
+      m->plan_cache->lists.arena = &c->arena;
+    }
     std::vector<int2> pairs;
     for (int r = 0; r < m->nspecies; ++r)
       for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
@@ -188,6 +196,7 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
                 const dbx_species *sp, const double *K, int nq, int mode,
                 double *out_I) {
   if (nq < 1) return dbx::fail(DBX_ERR_ARG, "nq must be >= 1");
+  c->arena.reset();  // the previous call ended synchronised
   if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_TC3 && mode != DBX_DEBYE_FP64 &&
       mode != DBX_DEBYE_FP32)
     return dbx::fail(DBX_ERR_ARG, "unknown Debye mode");
@@ -333,6 +342,7 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
                   const int64_t *ids, double rstep, const int64_t *nbins,
                   const dbx_species *sp, const double *K, int nq, double *out_I) {
   BatchState &b = c->batch;
+  c->arena.reset();  // the previous call ended synchronised
   const int nm = (int)ms.size();
   for (int i = 0; i < nm; ++i) DBX_TRY(alloc_hist(c, ms[i], nbins[i]));
   std::vector<const void *> hist_ptrs(nm);
@@ -544,6 +554,7 @@ int dbx_create(dbx_ctx **out, int device, size_t budget) {
       cudaSuccess)
     return DBX_ERR_CUDA;
   c->stream = c->own_stream;
+  c->hws.arena = c->tc.arena = c->batch.pref.arena = c->batch.hp.lists.arena = &c->arena;
   *out = c.release();
   return DBX_OK;
 }
@@ -686,6 +697,7 @@ int dbx_pair_histogram(dbx_ctx *c, int64_t id, int row, int col, double rstep,
   if (row < 0 || col < row || col >= m->nspecies)
     return set_err(c, dbx::fail(DBX_ERR_ARG, "need 0 <= row <= col < nspecies"));
   const int64_t pitch = pitch_of(nbins);
+  c->arena.reset();  // the previous call ended synchronised
   Error e = grow(c, &c->tmp_hist, sizeof(unsigned long long) * pitch);
   if (e.code) return set_err(c, e);
   dbx::HistPlan plan;
@@ -716,6 +728,7 @@ int dbx_histogram(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
   dbx::Model *m = find_model(c, id);
   if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
   c->tm.reset();
+  c->arena.reset();  // the previous call ended synchronised
   Error e = ensure_hist(c, m, rstep, nbins);
   if (e.code) return set_err(c, e);
   return set_err(c, copy_rows(c, m->d_hist, m->hist_pitch, nbins,
@@ -926,6 +939,7 @@ int dbx_run_deb(dbx_ctx *c, const char *deb_path, const char *out_prefix,
   } drop{c, id};
   const int64_t nbins = dbx_channels(d.rmax, d.rstep);
   dbx::Model *m = find_model(c, id);
+  c->arena.reset();  // the previous call ended synchronised
   Error e = ensure_hist(c, m, d.rstep, nbins);
   if (e.code) {
     if (verbose) printf("\nERROR: %s\n", e.msg.c_str());
