@@ -617,6 +617,13 @@ def run_engine(args):
                         "peak_basis": "hbm_gbs, %s" % pk_kind}
     flops = 2.0 * len(K) * m.nbins * npair_types
     tc_ach = flops / (ph["debye"] / 1e3) / 1e12
+    # bf16 MMA work the split form issues: per 128-row x 64-chunk x 256-bin
+    # tile, 10 digit-pair products of 2 x 128 x 64 x 256 FLOP
+    qp = (len(K) + 127) // 128 * 128
+    nch = (m.nbins + 255) // 256  # 256-bin chunks per pair type
+    col_tiles = npair_types * ((nch + 63) // 64)
+    issued = (2 * qp // 128) * col_tiles * 10 * 2.0 * 128 * 64 * 256
+    issued_tf = issued / (ph["debye"] / 1e3) / 1e12
     roof_tc = {"kernel": "gemm_persistent_kernel", "bound": "tensor",
                "achieved": tc_ach, "peak": pk["bf16_tflops"],
                "unit": "TFLOP/s", "frac": tc_ach / pk["bf16_tflops"],
@@ -624,7 +631,12 @@ def run_engine(args):
                "flops_basis": "2 x q x bins x pair types (one FP64-exact "
                               "sinc product per count); the split form "
                               "issues 10 bf16 MMAs per product",
-               "peak_basis": "bf16 dense, %s" % pk_kind}
+               "peak_basis": "bf16 dense, %s" % pk_kind,
+               "issued": {"achieved": issued_tf, "frac": issued_tf / pk["bf16_tflops"],
+                          "unit": "TFLOP/s",
+                          "basis": "bf16 MMA FLOP issued: 10 digit-pair products "
+                                   "per 128 x 64 x 256 tile, %d tiles" %
+                                   ((2 * qp // 128) * col_tiles)}}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
