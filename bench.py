@@ -236,12 +236,8 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, plain_models=None):
             ts.append(time.perf_counter() - t0)
         t_tc = float(np.median(ts))
         # every pattern's max relative error at every 10th q against the
-        # FP64 direct sum of its resident histograms
-        per = []
-        for i in range(len(mods)):
-            want = eng.intensity(hs[i], 1e-3, nb[i], mods[i].species,
-                                 K[::10], mode="fp64")
-            per.append(float(np.max(np.abs(I[i, ::10] - want) / np.abs(want))))
+        # FP64 direct sum of its resident histograms (dbx_pattern_errors)
+        per = eng.pattern_errors(hs, 1e-3, nb, sp, K, I, q_stride=10).tolist()
         worst = max(per)
         # plain form over a subset (it is slow), scaled per pattern
         sub = list(range(len(mods))) if plain_models is None else \

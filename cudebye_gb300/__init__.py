@@ -50,6 +50,7 @@ EXPORTS = (
     "dbx_k_grid", "dbx_atomic_prop", "dbx_intensity", "dbx_pattern",
     "dbx_set_stream", "dbx_set_timing", "dbx_get_timing", "dbx_get_traffic",
     "dbx_run_deb", "dbx_pair_histogram_noalloc", "dbx_patterns",
+    "dbx_pattern_errors",
     "dbx_set_graphs", "dbx_server_create", "dbx_server_submit",
     "dbx_server_wait", "dbx_server_stats", "dbx_server_destroy",
     "dbx_check_sqrt", "dbx_xyz2deb", "dbx_xyz2deb_defaults", "dbx_deb_pack",
@@ -167,6 +168,11 @@ def load_library(path=None):
                                         ctypes.c_double, i64p,
                                         ctypes.POINTER(Species), dp,
                                         ctypes.c_int, ctypes.c_int, dp]),
+        "dbx_pattern_errors": (ctypes.c_int, [c_p, i64p, ctypes.c_int,
+                                              ctypes.c_double, i64p,
+                                              ctypes.POINTER(Species), dp,
+                                              ctypes.c_int, dp, ctypes.c_int,
+                                              dp]),
         "dbx_set_graphs": (ctypes.c_int, [c_p, ctypes.c_int]),
         "dbx_check_sqrt": (ctypes.c_int, [c_p, ctypes.c_uint32, ctypes.c_uint32,
                                           i64p]),
@@ -477,6 +483,22 @@ class Engine:
             self.ctx, _ptr(ids, ctypes.c_int64), len(models), rstep,
             _ptr(nb, ctypes.c_int64), sp, _ptr(K, ctypes.c_double), K.size,
             MODES[mode], _ptr(out, ctypes.c_double)))
+        return out
+
+    def pattern_errors(self, models, rstep, nbins, species, K, I, q_stride=10):
+        """Max relative error of each row of I (patterns() of the same
+        arguments) against the FP64 direct sum at every q_stride-th q
+        (dbx_pattern_errors). Returns an array [nmodels]."""
+        K = np.ascontiguousarray(K, dtype=np.float64)
+        I = np.ascontiguousarray(I, dtype=np.float64)
+        ids = np.ascontiguousarray([m.id for m in models], dtype=np.int64)
+        nb = np.ascontiguousarray(nbins, dtype=np.int64)
+        sp = (Species * len(species))(*species)
+        out = np.zeros(len(models), dtype=np.float64)
+        self._check(self.lib.dbx_pattern_errors(
+            self.ctx, _ptr(ids, ctypes.c_int64), len(models), rstep,
+            _ptr(nb, ctypes.c_int64), sp, _ptr(K, ctypes.c_double), K.size,
+            _ptr(I, ctypes.c_double), int(q_stride), _ptr(out, ctypes.c_double)))
         return out
 
     def check_sqrt(self, lo_bits=0, hi_bits=0x7F800000):

@@ -818,6 +818,37 @@ int dbx_pattern(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
   return set_err(c, intensity(c, m, rstep, nbins, sp, K, nq, mode, out_I));
 }
 
+int dbx_pattern_errors(dbx_ctx *c, const int64_t *ids, int nmodels, double rstep,
+                       const int64_t *nbins, const dbx_species *sp, const double *K,
+                       int nq, const double *I, int q_stride, double *out_maxrel) {
+  if (!c || !ids || nmodels < 1 || !nbins || !sp || !K || nq < 1 || !I ||
+      q_stride < 1 || !out_maxrel || !(rstep > 0))
+    return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  std::vector<double> Ks, ref;
+  for (int q = 0; q < nq; q += q_stride) Ks.push_back(K[q]);
+  const int ns = (int)Ks.size();
+  ref.resize(ns);
+  int sp0 = 0;
+  for (int i = 0; i < nmodels; ++i) {
+    dbx::Model *m = find_model(c, ids[i]);
+    if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
+    c->tm.reset();
+    Error e = intensity(c, m, rstep, nbins[i], sp + sp0, Ks.data(), ns,
+                        DBX_DEBYE_FP64, ref.data());
+    if (e.code) return set_err(c, e);
+    double worst = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      const double r = ref[j], v = I[(size_t)i * nq + (size_t)j * q_stride];
+      if (r == 0.0 || !std::isfinite(r)) continue;
+      worst = std::max(worst, std::fabs(v - r) / std::fabs(r));
+    }
+    out_maxrel[i] = worst;
+    sp0 += m->nspecies;
+  }
+  return DBX_OK;
+}
+
 int dbx_set_graphs(dbx_ctx *c, int enable) {
   if (!c) return DBX_ERR_ARG;
   c->graphs = enable != 0;

@@ -216,6 +216,17 @@ int dbx_patterns(dbx_ctx *ctx, const int64_t *model_ids, int nmodels,
                  double rstep, const int64_t *nbins, const dbx_species *sp,
                  const double *K, int nq, int mode, double *out_I);
 
+/* Max relative error of each pattern of a batch (I = out_I of dbx_patterns
+ * with the same arguments, [nmodels][nq]) against the FP64 direct sum of
+ * the models' resident histograms (the reference's debyeRowSum arithmetic,
+ * cuDebye-v15.cu:493-538) at every q_stride-th q; q values where the FP64
+ * sum is 0 or not finite are skipped. out_maxrel[nmodels]. No counterpart
+ * in the reference, which has no error report. */
+int dbx_pattern_errors(dbx_ctx *ctx, const int64_t *model_ids, int nmodels,
+                       double rstep, const int64_t *nbins, const dbx_species *sp,
+                       const double *K, int nq, const double *I, int q_stride,
+                       double *out_maxrel);
+
 /* CUDA-graph replay of dbx_patterns (default on). */
 int dbx_set_graphs(dbx_ctx *ctx, int enable);
 

@@ -59,6 +59,35 @@ def test_batch_tc_matches_oracle_and_replays(engine, orc):
             h.free()
 
 
+def test_pattern_errors_report(engine, orc):
+    """dbx_pattern_errors: each pattern's max relative error against the FP64
+    direct sum at every 3rd q equals the error computed here against the
+    CPU FP64 oracle (to the oracle's agreement with the device FP64 sum),
+    and stays within 1e-6; a corrupted pattern is reported."""
+    mods = small_batch(47, n=4)
+    tt, K = mods[0].k_grid()
+    K = K[::7]
+    handles = [engine.upload(m.xyz, m.counts) for m in mods]
+    try:
+        nb = [m.nbins for m in mods]
+        sp = species_of(mods)
+        I = engine.patterns(handles, 1e-3, nb, sp, K)
+        err = engine.pattern_errors(handles, 1e-3, nb, sp, K, I, q_stride=3)
+        assert err.shape == (4,) and np.all(err <= 1e-6)
+        for m, h, row, e in zip(mods, handles, I, err):
+            want = orc.intensity(K[::3], engine.histogram(h, m.rstep, m.nbins),
+                                 m.species, m.rstep)
+            mine = float(np.max(np.abs(row[::3] - want) / np.abs(want)))
+            assert abs(mine - e) <= 1e-10, (mine, e)
+        bad = I.copy()
+        bad[2, 3] *= 1.001
+        err2 = engine.pattern_errors(handles, 1e-3, nb, sp, K, bad, q_stride=3)
+        assert err2[2] >= 9e-4 and np.allclose(err2[[0, 1, 3]], err[[0, 1, 3]])
+    finally:
+        for h in handles:
+            h.free()
+
+
 def test_batch_result_independent_of_batch_mates(engine):
     """A model's pattern is the same alone and inside a batch."""
     mods = small_batch(42, n=5)
