@@ -570,7 +570,7 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
     {
       double cd = 0, co = 0;
       const int nI = I1 - I0;
-      for (int smp = 0; smp < 4096 && nI > 0; ++smp) {
+      for (int smp = 0; smp < 4096 && nitems > 0; ++smp) {  // nitems: both non-empty
         const int I = I0 + (int)((int64_t)smp * nI / 4096);
         const int Jlo = (a == b) ? I : Jb0;
         const int J = Jlo + (int)(((int64_t)smp * 7919) % std::max(1, Jb1 - Jlo));

@@ -40,6 +40,17 @@ def test_empty_species(engine, orc):
     assert h[1].sum() == 0 and h[3].sum() == 0 and h[4].sum() == 0  # 01, 11, 12
 
 
+def test_empty_species_many_windows(engine, orc):
+    """Empty species in a histogram of several windows (the planner samples
+    tile pairs of every non-empty species pair to choose the windows)."""
+    rng = np.random.default_rng(11)
+    xyz = rng.uniform(-6, 6, (500, 3)).astype(np.float32)
+    K = cd.k_grid(1.5406, 10, 130, 2.0)[1]
+    h = check(engine, orc, xyz, [0, 200, 0, 300, 0], 5e-5,
+              cd.channels(25, 5e-5), sp(["O", "Al", "Mg", "Fe", "O"]), K)
+    assert h.shape[0] == 15 and h[0].sum() == 0
+
+
 def test_coincident_atoms(engine, orc):
     rng = np.random.default_rng(2)
     base = rng.uniform(-5, 5, (150, 3)).astype(np.float32)
