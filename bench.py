@@ -475,6 +475,54 @@ def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, pool=32,
                       "submit to result (incl. upload, queueing, readback)"}
 
 
+def reference_program(m, block=16, grid=4096, timeout=900):
+    """The reference's own CUDA program (cuDebye-v15.cu, built from an
+    edited copy by `make -C oracle ref`: CUDA 13 / gcc fixes, --fmad=false)
+    run once on this workload as a GPU timing beside the CPU arm. The
+    workload is written as a .deb with hist 0 (intensities only, so no
+    .debx writing inside its compute phase) and the launch grid `block`,
+    `grid` of its line 1. Reported: the process wall time and the phases the
+    program prints itself (cuDebye-v15.cu:840, :922, :971; clock(), i.e.
+    process CPU time, which its synchronous spin waits keep close to wall
+    time)."""
+    import re
+    import shutil
+    import tempfile
+    from oracle import pyoracle
+    if not os.path.exists(pyoracle.REF_BIN):
+        return {"unavailable": "reference program not built (its source "
+                               "copy was never made here)"}
+    tmp = tempfile.mkdtemp(prefix="dbx_refprog_")
+    try:
+        deb = os.path.join(tmp, "w.deb")
+        m.write_deb(deb, block=block, grid=grid, hist=0)
+        t0 = time.perf_counter()
+        r = subprocess.run([pyoracle.REF_BIN, deb], capture_output=True,
+                           encoding="latin-1", timeout=timeout)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            return {"unavailable": "reference program exit %d: %s"
+                    % (r.returncode, (r.stdout + r.stderr)[-300:])}
+
+        def phase(label):
+            g = re.search(label + r"\s*([0-9.eE+-]+) s", r.stdout)
+            return float(g.group(1)) if g else None
+        load = phase(r"Time for Loading the Input File:")
+        alloc = phase(r"Time for Allocating the necessary Memory on the Device:")
+        calc = phase(r"Evaluation of the Debye Double Sum:")
+        I = np.loadtxt(deb + "I")[:, 1]
+        return {"program": "cuDebye-v15.cu, CUDA 13 edits, nvcc --fmad=false, sm_103a",
+                "deb_line1": "0 %d %d" % (block, grid), "hist": 0,
+                "wall_s": wall, "load_s": load, "alloc_s": alloc,
+                "compute_s": calc,
+                "value": m.pairs / calc / 1e9 if calc else None,
+                "unit": METRIC,
+                "warnings": r.stdout.count("WARNING"),
+                "intensity_sum": float(np.sum(I))}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -508,6 +556,8 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0},
         "wall_s": wall,
     }
+    if not args.no_refprog:
+        line["reference_program_gpu"] = reference_program(m)
     print(json.dumps(line))
     return 0
 
@@ -695,6 +745,9 @@ def main():
                     help="skip the file-surface timings")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the 20,000-point precision comparison")
+    ap.add_argument("--no-refprog", action="store_true",
+                    help="reference arm: skip the reference's own CUDA "
+                         "program run")
     ap.add_argument("--serve-seconds", type=float, default=6.0,
                     help="seconds of Poisson arrivals per rate")
     args = ap.parse_args()

@@ -14,6 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liborc.so")
 CLI = os.path.join(BUILD, "orc_debye")
+# The reference program (cuDebye-v15.cu built by `make -C oracle ref`)
+REF_BIN = os.path.join(HERE, "_ref", "cudebye_ref")
 
 _lib = None
 
@@ -25,6 +27,25 @@ def build():
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
     return LIB
+
+
+def build_ref_start():
+    """Start `make -C oracle ref` (nvcc, about 20 s) in the background;
+    finish with build_ref_finish(). Nothing is built where neither the
+    reference's source nor its edited copy is present."""
+    return subprocess.Popen(["make", "-s", "-C", HERE, "ref"],
+                            stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                            text=True)
+
+
+def build_ref_finish(proc):
+    """Wait for build_ref_start's make; returns REF_BIN if it exists. A
+    failed build leaves the reference program's tests skipped, not the
+    engine's build failed, so its output is printed."""
+    out, _ = proc.communicate()
+    if proc.returncode != 0:
+        print("reference program build failed:\n" + out)
+    return REF_BIN if os.path.exists(REF_BIN) else None
 
 
 def lib():
