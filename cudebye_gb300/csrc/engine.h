@@ -95,8 +95,14 @@ Error buf_grow(DevBuf *b, size_t bytes, size_t *delta, cudaStream_t stream);
 // a tile pair covers a narrow window of distances.
 constexpr int kTile = 128;
 
+// Bounding box of a tile, and of its column quarters (atoms [32 q, 32 q +
+// 32), the columns one pass of a warp's lanes reads), for the planner of
+// multi-window histograms. A box with a NaN coordinate is all NaN; an empty
+// quarter is (+inf, -inf).
+constexpr int kQuarter = 32;
 struct TileBox {
   float lo[3], hi[3];
+  float qlo[4][3], qhi[4][3];
 };
 
 struct Model {
@@ -167,10 +173,12 @@ struct HistSeg {  // one (model, pair, bin window) accumulated in smem
   int wl;                   // window length in bins
   int task_begin, task_end;
   unsigned nbins;           // bins of this histogram
-  // Item source: kSegList reads {I, J | diag << 31} from the plan's item
-  // list; kSegRect enumerates tiles ti0 + [0, tni) x tj0 + [0, tnj) and
-  // kSegTri the pairs I <= J of ti0 + [0, tni) (a species with itself),
-  // item index = task-local position.
+  // Item source: kSegList reads {I | q0 << 25 | (4 - q1) << 27, J | diag
+  // << 31} from the plan's item list (the item covers the columns of
+  // quarters [q0, q1) of tile J: all of them when the bits are 0);
+  // kSegRect enumerates tiles ti0 + [0, tni) x tj0 + [0, tnj) and kSegTri
+  // the pairs I <= J of ti0 + [0, tni) (a species with itself), item index
+  // = task-local position.
   int shape;
   int ti0, tni, tj0, tnj;
   // Bins of the window this segment counts, window-relative: [own_lo,
@@ -180,6 +188,8 @@ struct HistSeg {  // one (model, pair, bin window) accumulated in smem
   int own_lo, own_len;
 };
 constexpr int kSegList = 0, kSegRect = 1, kSegTri = 2;
+constexpr int kItemQ0Shift = 25, kItemQ1Shift = 27;
+constexpr int kItemTileMask = (1 << 25) - 1;
 struct HistTask {  // one CTA-sized slice of a segment's tile pairs
   int seg;
   int item_begin, item_end;

@@ -213,8 +213,12 @@ __global__ void __launch_bounds__(kHistThreads, 1)
          it_i += kHistThreads / 32) {
       const int2 it = seg_item(sg, items, it_i);
       const bool diag = it.y < 0;
-      const int2 TI = __ldg(&tiles[it.x]);
+      const unsigned ix = (unsigned)it.x;
+      const int2 TI = __ldg(&tiles[ix & (unsigned)kItemTileMask]);
       const int2 TJ = __ldg(&tiles[it.y & 0x7fffffff]);
+      // columns [jb, je): the item's quarters of tile J
+      const int jb = kQuarter * (int)((ix >> kItemQ0Shift) & 3u);
+      const int je = min(TJ.y, kQuarter * (4 - (int)((ix >> kItemQ1Shift) & 3u)));
       float x[4], y[4], z[4];
       int jlim[4];
 #pragma unroll
@@ -225,24 +229,25 @@ __global__ void __launch_bounds__(kHistThreads, 1)
         x[r] = a.x;
         y[r] = a.y;
         z[r] = a.z;
-        // diag tile: pairs j <= i incl. i == j (cuDebye-v15.cu:137)
-        jlim[r] = act ? (diag ? pi : 0x7fffffff) : -1;
+        // diag tile: pairs j <= i incl. i == j (cuDebye-v15.cu:137); the
+        // loop counts columns from jb
+        jlim[r] = act ? (diag ? pi - jb : 0x7fffffff) : -1;
       }
-      const float4 *bj = atoms + TJ.x;
+      const float4 *bj = atoms + TJ.x + jb;
       const bool all_valid = !diag && TI.y == kTile;  // warp-uniform
       if (all_valid) {
         if (full_window)
-          pair_loop<true, true>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+          pair_loop<true, true>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
                                 nbins, pgh, pvo, pvi, pvend, oor_total);
         else
-          pair_loop<true, false>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+          pair_loop<true, false>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
                                  nbins, pgh, pvo, pvi, pvend, oor_total);
       } else {
         if (full_window)
-          pair_loop<false, true>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+          pair_loop<false, true>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
                                  nbins, pgh, pvo, pvi, pvend, oor_total);
         else
-          pair_loop<false, false>(bj, TJ.y, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
+          pair_loop<false, false>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
                                   nbins, pgh, pvo, pvi, pvend, oor_total);
       }
     }
@@ -486,6 +491,8 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
     }
     if (m.boxes.size() != m.tiles.size())
       return fail(DBX_ERR_ARG, "tile boxes are not on the host");
+    if (m.tile_start[a + 1] > kItemTileMask + 1)
+      return fail(DBX_ERR_ARG, "too many tiles in one model for a multi-window histogram");
     // Tile pairs listed per window from their bounding boxes, rows of tiles
     // split among host threads by item count; the lists are joined in row
     // order, so the plan does not depend on the thread count.
@@ -601,13 +608,48 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       };
       for (int I = row_cut[t]; I < row_cut[t + 1]; ++I) {
         const int2 TI = m.tiles[I];
+        const TileBox &BI = m.boxes[I];
         for (int J = (a == b) ? I : Jb0; J < Jb1; ++J) {
           const bool diag = (a == b) && (I == J);
           const int2 it = make_int2(I, J | (diag ? int(0x80000000u) : 0));
-          const int np = (int)item_pairs(TI.y, m.tiles[J].y, diag);
+          const int nJ = m.tiles[J].y;
+          const int np = (int)item_pairs(TI.y, nJ, diag);
           int64_t kmin, kmax;
-          box_bins(m.boxes[I], m.boxes[J], inv, &kmin, &kmax);
-          assign(g, kmin, kmax, [&](int64_t l) { put(l, it, np); });
+          box_bins(BI, m.boxes[J], inv, &kmin, &kmax);
+          // In an owned list the item runs only over the columns whose
+          // quarters reach the window's owned bins (their bin ranges from
+          // the quarter boxes, computed on first use).
+          int64_t qk0[4], qk1[4];
+          int nq = -1;
+          assign(g, kmin, kmax, [&](int64_t l) {
+            if (!(l & 1)) {
+              put(l, it, np);
+              return;
+            }
+            if (nq < 0) {
+              nq = (nJ + kQuarter - 1) / kQuarter;
+              for (int q = 0; q < nq; ++q) {
+                TileBox Q;
+                for (int d = 0; d < 3; ++d) {
+                  Q.lo[d] = m.boxes[J].qlo[q][d];
+                  Q.hi[d] = m.boxes[J].qhi[q][d];
+                }
+                box_bins(BI, Q, inv, &qk0[q], &qk1[q]);
+              }
+            }
+            const int64_t w = l / 2, lo = own[w], hi = own[w + 1];
+            unsigned mask = 0;
+            for (int q = 0; q < nq; ++q)  // the last window counts bins >= nbins
+              if (qk1[q] >= lo && (w == nwin - 1 || std::max<int64_t>(qk0[q], 0) < hi))
+                mask |= 1u << q;
+            if (!mask) return;
+            const int q0 = __builtin_ctz(mask), q1 = 32 - __builtin_clz(mask);
+            const int jb = q0 * kQuarter, je = std::min(nJ, q1 * kQuarter);
+            const int2 itq = make_int2(I | (q0 << kItemQ0Shift) | ((4 - q1) << kItemQ1Shift), it.y);
+            const int npq = diag ? (je - jb) * TI.y - (jb + je - 1) * (je - jb) / 2
+                                 : (je - jb) * TI.y;
+            put(l, itq, npq);
+          });
         }
       }
     };

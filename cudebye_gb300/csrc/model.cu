@@ -80,22 +80,30 @@ static void sort_species(const float *const xyz[3], int64_t start, int64_t n,
   for (int64_t t0 = 0; t0 < n; t0 += kTile) {
     const int cnt = (int)std::min<int64_t>(kTile, n - t0);
     TileBox bx;
-    for (int d = 0; d < 3; ++d) {
-      bx.lo[d] = INFINITY;
-      bx.hi[d] = -INFINITY;
-    }
     bool nan = false;
-    for (int i = 0; i < cnt; ++i) {
-      const float4 a = atoms[start + t0 + i];
-      const float v[3] = {a.x, a.y, a.z};
+    for (int q = 0; q < 4; ++q) {
+      bool qnan = false;
       for (int d = 0; d < 3; ++d) {
-        nan |= v[d] != v[d];
-        bx.lo[d] = std::min(bx.lo[d], v[d]);
-        bx.hi[d] = std::max(bx.hi[d], v[d]);
+        bx.qlo[q][d] = INFINITY;
+        bx.qhi[q][d] = -INFINITY;
       }
+      for (int i = q * kQuarter; i < std::min(cnt, (q + 1) * kQuarter); ++i) {
+        const float4 a = atoms[start + t0 + i];
+        const float v[3] = {a.x, a.y, a.z};
+        for (int d = 0; d < 3; ++d) {
+          qnan |= v[d] != v[d];
+          bx.qlo[q][d] = std::min(bx.qlo[q][d], v[d]);
+          bx.qhi[q][d] = std::max(bx.qhi[q][d], v[d]);
+        }
+      }
+      if (qnan)  // a NaN atom's distances are unknown: the box says so
+        for (int d = 0; d < 3; ++d) bx.qlo[q][d] = bx.qhi[q][d] = NAN;
+      nan |= qnan;
     }
-    if (nan)  // a NaN atom's distances are unknown: the box says so
-      for (int d = 0; d < 3; ++d) bx.lo[d] = bx.hi[d] = NAN;
+    for (int d = 0; d < 3; ++d) {
+      bx.lo[d] = nan ? NAN : std::min({bx.qlo[0][d], bx.qlo[1][d], bx.qlo[2][d], bx.qlo[3][d]});
+      bx.hi[d] = nan ? NAN : std::max({bx.qhi[0][d], bx.qhi[1][d], bx.qhi[2][d], bx.qhi[3][d]});
+    }
     boxes->push_back(bx);
   }
 }

@@ -219,7 +219,9 @@ __global__ void gather_kernel(const float *__restrict__ xyz, long long n,
   atoms[j] = make_float4(xyz[src], xyz[n + src], xyz[2 * n + src], 0.f);
 }
 
-// Bounding box of every tile (one warp per tile; tiles {first, count}).
+// Bounding box of every tile and of its column quarters (one warp per
+// tile, one quarter of 32 atoms per pass; tiles {first, count}), as the
+// host computes them.
 __global__ void tile_boxes_kernel(const float4 *__restrict__ atoms,
                                   const int2 *__restrict__ tiles, int ntiles,
                                   TileBox *__restrict__ boxes) {
@@ -227,25 +229,36 @@ __global__ void tile_boxes_kernel(const float4 *__restrict__ atoms,
   const int lane = threadIdx.x & 31;
   if (t >= ntiles) return;
   const int2 tl = tiles[t];
+  TileBox b;
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   bool nan = false;
-  for (int i = lane; i < tl.y; i += 32) {
-    const float4 a = atoms[tl.x + i];
-    const float v[3] = {a.x, a.y, a.z};
+  for (int q = 0; q < 4; ++q) {
+    const int i = q * kQuarter + lane;
+    float ql[3] = {INFINITY, INFINITY, INFINITY}, qh[3] = {-INFINITY, -INFINITY, -INFINITY};
+    bool qn = false;
+    if (i < tl.y) {
+      const float4 a = atoms[tl.x + i];
+      const float v[3] = {a.x, a.y, a.z};
+      for (int d = 0; d < 3; ++d) {
+        qn |= v[d] != v[d];
+        ql[d] = fminf(ql[d], v[d]);
+        qh[d] = fmaxf(qh[d], v[d]);
+      }
+    }
+    qn = __any_sync(0xffffffffu, qn);
     for (int d = 0; d < 3; ++d) {
-      nan |= v[d] != v[d];
-      lo[d] = fminf(lo[d], v[d]);
-      hi[d] = fmaxf(hi[d], v[d]);
+      for (int off = 16; off > 0; off >>= 1) {
+        ql[d] = fminf(ql[d], __shfl_xor_sync(0xffffffffu, ql[d], off));
+        qh[d] = fmaxf(qh[d], __shfl_xor_sync(0xffffffffu, qh[d], off));
+      }
+      b.qlo[q][d] = qn ? NAN : ql[d];  // a NaN atom gets a NaN box, as on the host
+      b.qhi[q][d] = qn ? NAN : qh[d];
+      lo[d] = fminf(lo[d], ql[d]);
+      hi[d] = fmaxf(hi[d], qh[d]);
     }
+    nan |= qn;
   }
-  nan = __any_sync(0xffffffffu, nan);
-  for (int d = 0; d < 3; ++d)
-    for (int off = 16; off > 0; off >>= 1) {
-      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
-      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
-    }
   if (lane == 0) {
-    TileBox b;  // a tile with a NaN atom gets a NaN box, as on the host
     for (int d = 0; d < 3; ++d) {
       b.lo[d] = nan ? NAN : lo[d];
       b.hi[d] = nan ? NAN : hi[d];
