@@ -523,6 +523,30 @@ def reference_program(m, block=16, grid=4096, timeout=900):
         shutil.rmtree(tmp, ignore_errors=True)
 
 
+def reference_program_batch(step=16, seed=3):
+    """The reference program on every `step`-th model of the 256-model mix,
+    one process per model (how the reference's multisim runs a folder of
+    models), as a GPU timing beside the batched engine: patterns/s over the
+    program's own compute phases and over the processes' wall time."""
+    from cudebye_gb300 import lattice
+    models = lattice.batch256(seed=seed)[::step]
+    runs = []
+    for m in models:
+        r = reference_program(m)
+        if "unavailable" in r:
+            return r
+        runs.append(r)
+    comp = sum(r["compute_s"] for r in runs)
+    wall = sum(r["wall_s"] for r in runs)
+    return {"models": len(runs),
+            "sample": "every %dth model of the 256-model mix (seed %d), "
+                      "hist 0, line 1 '0 16 4096'" % (step, seed),
+            "binned_pairs": int(sum(m.pairs for m in models)),
+            "compute_s": comp, "wall_s": wall,
+            "patterns_per_s_compute": len(runs) / comp,
+            "patterns_per_s_process": len(runs) / wall}
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -558,6 +582,7 @@ def run_reference(args):
     }
     if not args.no_refprog:
         line["reference_program_gpu"] = reference_program(m)
+        line["reference_program_gpu_batch256"] = reference_program_batch()
     print(json.dumps(line))
     return 0
 

@@ -54,7 +54,7 @@ EXPORTS = (
     "dbx_set_graphs", "dbx_server_create", "dbx_server_submit",
     "dbx_server_wait", "dbx_server_stats", "dbx_server_destroy",
     "dbx_check_sqrt", "dbx_xyz2deb", "dbx_xyz2deb_defaults", "dbx_deb_pack",
-    "dbx_run_dir",
+    "dbx_run_dir", "dbx_curve_index",
 )
 TIMERS = ("hist", "hist_reduce", "prefactor", "debye", "pass")
 
@@ -141,6 +141,7 @@ def load_library(path=None):
         "dbx_histogram": (ctypes.c_int, [c_p, ctypes.c_int64, ctypes.c_double,
                                          ctypes.c_int64, i64p]),
         "dbx_channels": (ctypes.c_int64, [ctypes.c_double, ctypes.c_double]),
+        "dbx_curve_index": (ctypes.c_int64, [ctypes.c_uint32] * 3 + [ctypes.c_int]),
         "dbx_reduce_check": (ctypes.c_int, [i64p, ctypes.c_int64,
                                             ctypes.c_double, ctypes.c_int64,
                                             ctypes.c_int64, ctypes.c_int, i64p]),
@@ -213,6 +214,12 @@ def _ptr(a, ct):
 def channels(rmax, rstep):
     """int(rmax/rstep)+2 (cuDebye-v15.cu:732)."""
     return int(rmax / rstep) + 2
+
+
+def curve_index(x, y, z, bits):
+    """Position of grid cell (x, y, z) along the Hilbert curve that orders
+    each species' atoms into tiles (dbx_curve_index; -1 if out of range)."""
+    return int(load_library().dbx_curve_index(x, y, z, bits))
 
 
 def k_grid(lam, tt_min, tt_max, tt_step):

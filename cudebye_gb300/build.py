@@ -27,7 +27,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # distance arithmetic into FMAs (it also uses explicit _rn intrinsics).
 EXTRA = {"hist.cu": ["--fmad=false"], "hist_noalloc.cu": ["--fmad=false"]}
 LIB_SOURCES = ["hist.cu", "hist_noalloc.cu", "debye.cu", "debye_tc.cu",
-               "model.cu", "morton.cu", "capi.cu", "serve.cu", "debio.cpp",
+               "model.cu", "spatial_sort.cu", "capi.cu", "serve.cu", "debio.cpp",
                "xyz2deb.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 

@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "curve.cuh"
 #include "debio.h"
 #include "debye_tc.h"
 #include "engine.h"
@@ -686,6 +687,11 @@ int dbx_model_free(dbx_ctx *c, int64_t id) {
 
 int64_t dbx_channels(double rmax, double rstep) {
   return (int64_t)(int)(rmax / rstep) + 2;  // cuDebye-v15.cu:732
+}
+
+int64_t dbx_curve_index(uint32_t x, uint32_t y, uint32_t z, int bits) {
+  if (bits < 1 || bits > 10 || ((x | y | z) >> bits) != 0) return -1;
+  return (int64_t)dbx::hilbert3(x, y, z, bits);
 }
 
 int dbx_pair_histogram(dbx_ctx *c, int64_t id, int row, int col, double rstep,

@@ -90,7 +90,7 @@ Error h2d_copy(void *dst, const void *src, size_t n, cudaStream_t stream,
 Error buf_grow(DevBuf *b, size_t bytes, size_t *delta, cudaStream_t stream);
 
 // ---- resident model -------------------------------------------------------
-// Atoms are stored per species, each species sorted along a Morton curve
+// Atoms are stored per species, each species sorted along a Hilbert curve
 // and cut into tiles of kTile atoms, so that a tile is spatially compact and
 // a tile pair covers a narrow window of distances.
 constexpr int kTile = 128;
@@ -145,7 +145,7 @@ size_t model_upload_bytes(const Model &m);
 Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
                       PinArena *arena = nullptr);
 size_t model_device_bytes(const Model &m);  // atoms, tiles, hist, plan
-// Sort and upload on the device (morton.cu): the same atoms, tiles and
+// Sort and upload on the device (spatial_sort.cu): the same atoms, tiles and
 // boxes as model_prepare + model_to_device; `pin` is pinned host memory
 // of at least 3 natoms floats; the tile boxes stay on the device
 // (d_boxes) until model_host_boxes copies them for a multi-window plan.

@@ -5,8 +5,8 @@
 // uint32 atomicAdd and synchronise the host after every 67M-pair launch.
 //
 // Design:
-//  * Atoms of each species are Morton-sorted and cut into tiles of 128
-//    (capi.cu); a work item is one tile pair.
+//  * Atoms of each species are sorted along a Hilbert curve and cut into
+//    tiles of 128 (model.cu, spatial_sort.cu); a work item is one tile pair.
 //  * A CTA owns a window of up to ~114k bins held in shared memory as packed
 //    16-bit counters (two bins per 32-bit word). A counter that wraps is
 //    detected from the atomic's return value and compensated exactly in the

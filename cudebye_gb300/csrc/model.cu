@@ -7,22 +7,13 @@
 #include <thread>
 #include <vector>
 
+#include "curve.cuh"
 #include "engine.h"
 
 namespace dbx {
 
-// Interleave the low 10 bits of v with two zero bits between each.
-static uint32_t spread10(uint32_t v) {
-  v &= 0x3ffu;
-  v = (v | (v << 16)) & 0x030000FFu;
-  v = (v | (v << 8)) & 0x0300F00Fu;
-  v = (v | (v << 4)) & 0x030C30C3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
-}
-
-// One species: Morton order of its atoms on a grid over the species'
-// bounding cube with about 2 cells per atom (16^3 to 1024^3 cells; stable
+// One species: Hilbert order (curve.cuh) of its atoms on a grid over the
+// species' bounding cube with about 2 cells per atom (16^3 to 1024^3 cells; stable
 // LSD radix sort in passes of up to 11 bits, so atoms with equal codes keep
 // their input order), written to atoms[start..start+n), and the bounding
 // boxes of its tiles of kTile atoms. Any order gives the same histograms; a
@@ -52,7 +43,7 @@ static void sort_species(const float *const xyz[3], int64_t start, int64_t n,
       t = t >= 0.f ? (t <= top ? t : top) : 0.f;  // NaN -> 0
       q[d] = (uint32_t)t;
     }
-    code[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+    code[i] = hilbert3(q[0], q[1], q[2], bits);
     idx[i] = (int32_t)i;
   }
   const int total = 3 * bits;

@@ -1,7 +1,7 @@
-// morton.cu — the spatial sort of a model's atoms on the device.
+// spatial_sort.cu — the spatial sort of a model's atoms on the device.
 //
-// The same order as the host path (model_prepare): per species, Morton
-// codes on a grid over the species' bounding cube with about 2 cells per
+// The same order as the host path (model_prepare): per species, Hilbert
+// indices (curve.cuh) on a grid over the species' bounding cube with about 2 cells per
 // atom, sorted stably (equal codes keep their input order), so a model
 // uploaded either way has the same atoms, tiles and boxes. Used by
 // dbx_model_upload for large models, where the host sort would dominate
@@ -15,6 +15,7 @@
 #include <cstring>
 #include <vector>
 
+#include "curve.cuh"
 #include "engine.h"
 
 namespace dbx {
@@ -23,15 +24,6 @@ namespace {
 constexpr int kSortThreads = 256;
 constexpr int kSortChunk = 4096;  // keys per block and pass (16 per thread)
 constexpr int kRadix = 256;
-
-__device__ __forceinline__ uint32_t spread10_d(uint32_t v) {
-  v &= 0x3ffu;
-  v = (v | (v << 16)) & 0x030000FFu;
-  v = (v | (v << 8)) & 0x0300F00Fu;
-  v = (v | (v << 4)) & 0x030C30C3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
-}
 
 // Species of global atom index i (species ranges start[0..ns]).
 __device__ __forceinline__ int species_of(long long i, const long long *start,
@@ -81,7 +73,7 @@ __global__ void bbox_kernel(const float *__restrict__ xyz, long long n,
   }
 }
 
-// Morton key of every atom: bits 32.. the species, bits 0..31 the code
+// Sort key of every atom: bits 32.. the species, bits 0..31 the code
 // computed exactly as the host does (FP32, IEEE operations).
 __global__ void keys_kernel(const float *__restrict__ xyz, long long n,
                             const long long *__restrict__ start, int ns,
@@ -108,8 +100,7 @@ __global__ void keys_kernel(const float *__restrict__ xyz, long long n,
     t = t >= 0.f ? (t <= top ? t : top) : 0.f;  // NaN -> 0
     q[d] = (uint32_t)t;
   }
-  const uint32_t code =
-      spread10_d(q[0]) | (spread10_d(q[1]) << 1) | (spread10_d(q[2]) << 2);
+  const uint32_t code = hilbert3(q[0], q[1], q[2], bits[s]);
   key[i] = ((unsigned long long)s << 32) | code;
   idx[i] = (int)(i - start[s]);
 }

@@ -150,6 +150,12 @@ int dbx_pair_histogram_noalloc(const float *x, const float *y, const float *z,
 /* int(rmax/rstep)+2 (cuDebye-v15.cu:732). */
 int64_t dbx_channels(double rmax, double rstep);
 
+/* Position of grid cell (x, y, z) (each < 2^bits, 1 <= bits <= 10) along
+ * the Hilbert curve that orders each species' atoms into tiles (the
+ * layout the upload builds; the reference keeps input order,
+ * cuDebye-v15.cu:819-827). Host only; -1 for arguments out of range. */
+int64_t dbx_curve_index(uint32_t x, uint32_t y, uint32_t z, int bits);
+
 /* Self-checks of reduceCheck (cuDebye-v15.cu:360-410) on one pair
  * histogram: expected total n_a(n_a+1)/2 (diag) or n_a*n_b, bin 0 == n_a
  * (diag), and the count of distances below 0.25 A beyond the self pairs

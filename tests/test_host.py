@@ -61,6 +61,30 @@ def test_host_entry_points_without_gpu(built_lib):
         assert rc == -2 and not ctx
 
 
+def test_tile_order_is_a_hilbert_curve(built_lib):
+    """The curve that orders atoms into tiles visits every cell of the
+    2^bits cube once, each step to a face neighbour (so runs of it, the
+    tiles, are connected and compact)."""
+    cd.load_library(built_lib)
+    for bits in (1, 2, 3, 4):
+        n = 1 << bits
+        cells = {}
+        for x in range(n):
+            for y in range(n):
+                for z in range(n):
+                    cells[cd.curve_index(x, y, z, bits)] = (x, y, z)
+        assert sorted(cells) == list(range(n ** 3)), bits
+        for k in range(n ** 3 - 1):
+            step = sum(abs(a - b) for a, b in zip(cells[k], cells[k + 1]))
+            assert step == 1, (bits, k, cells[k], cells[k + 1])
+    # the largest grid the sort uses: corners and a sample stay in range
+    top = (1 << 10) - 1
+    for c in [(0, 0, 0), (top, top, top), (top, 0, 517), (3, 900, 12)]:
+        assert 0 <= cd.curve_index(*c, 10) < 1 << 30
+    assert cd.curve_index(1 << 10, 0, 0, 10) == -1
+    assert cd.curve_index(0, 0, 0, 11) == -1
+
+
 def test_k_grid_matches_oracle(orc):
     for grid in [(1.5418, 10.0, 140.0, 0.02), (1.5406, 10.0, 130.0, 0.02),
                  (0.7107, 5.0, 150.0, 145.0 / 19999)]:
