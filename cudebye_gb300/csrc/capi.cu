@@ -207,12 +207,13 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   DBX_TRY(grow(c, &c->K, sizeof(double) * nq));
   DBX_TRY(grow(c, &c->ff, sizeof(double) * nq * (size_t)np));
   DBX_TRY(grow(c, &c->I, sizeof(double) * nq));
-  DBX_CUDA_TRY(cudaMemcpyAsync(c->K.p, K, sizeof(double) * nq,
-                               cudaMemcpyHostToDevice, c->stream));
+  // through the pinned arena: a copy from pageable memory would hold the
+  // host until the histogram queued before it has run
+  DBX_TRY(dbx::h2d_copy(c->K.p, K, sizeof(double) * nq, c->stream, &c->arena));
   c->h2d += sizeof(double) * nq + sizeof(dbx_species) * m->nspecies;
   c->tm.start(DBX_T_PREFACTOR, c->stream);
   DBX_TRY(dbx::debye_prefactor(sp, m->nspecies, (const double *)c->K.p, nq,
-                               (double *)c->ff.p, c->stream));
+                               (double *)c->ff.p, c->stream, &c->arena));
   c->tm.stop(DBX_T_PREFACTOR, c->stream);
   if (mode == DBX_DEBYE_TC || mode == DBX_DEBYE_TC3) {
     std::vector<dbx::TcCol> cols(np);

@@ -80,7 +80,7 @@ __global__ void debye_prefactor_kernel(const SpeciesDev *__restrict__ sp,
 }
 
 Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
-                      int nq, double *d_ff, cudaStream_t stream) {
+                      int nq, double *d_ff, cudaStream_t stream, PinArena *arena) {
   static_assert(sizeof(SpeciesDev) == sizeof(dbx_species), "layout");
   SpeciesDev *d_sp = nullptr;
   double *d_F = nullptr;
@@ -88,9 +88,16 @@ Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
                                stream));
   cudaError_t e = cudaMallocAsync((void **)&d_F,
                                   sizeof(double) * nq * (size_t)nspecies, stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_sp, sp, sizeof(SpeciesDev) * nspecies,
+  if (e == cudaSuccess) {
+    const void *from = sp;
+    if (arena)
+      if (void *p = arena->take(sizeof(SpeciesDev) * nspecies)) {
+        std::memcpy(p, sp, sizeof(SpeciesDev) * nspecies);
+        from = p;
+      }
+    e = cudaMemcpyAsync(d_sp, from, sizeof(SpeciesDev) * nspecies,
                         cudaMemcpyHostToDevice, stream);
+  }
   if (e == cudaSuccess) {
     species_f_kernel<<<dim3((nq + 127) / 128, nspecies), 128, 0, stream>>>(
         d_sp, nullptr, d_K, nq, d_F);

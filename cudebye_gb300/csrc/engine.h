@@ -301,8 +301,10 @@ Error prefactor_upload(PrefState *st, const dbx_species *sp, int nsp,
 Error prefactor_execute(const PrefState &st, const double *d_K, int nq,
                         double *d_ff, cudaStream_t stream);
 // out_ff[p][q] for every pair of the model's species.
+// (the species go to the device through `arena` when it is not null)
 Error debye_prefactor(const dbx_species *sp, int nspecies, const double *d_K,
-                      int nq, double *d_ff, cudaStream_t stream);
+                      int nq, double *d_ff, cudaStream_t stream,
+                      PinArena *arena = nullptr);
 // I[q] = sum_p ff[p][q] * sum_k m_k sinc(K r_k) over the model's histograms.
 Error debye_direct(int mode, const unsigned long long *d_hist, int npairs,
                    int64_t pitch, int64_t nbins, double rstep,
