@@ -80,6 +80,33 @@ class Clocks:
         self.index = index
         self.proc = None
         self.lines = []
+        self.first = 0
+        self.last = None
+
+    def start(self, wait_s=5.0):
+        """Start sampling before the warm-up, so that nvidia-smi's own
+        start-up (driver queries while it initialises) stays out of the timed
+        steps, and wait for its first line."""
+        import atexit
+        self.__enter__()
+        atexit.register(self.__exit__)  # the sampler ends with the process
+        t0 = time.time()
+        while self.proc and not self.lines and time.time() - t0 < wait_s:
+            time.sleep(0.01)
+        return self
+
+    def mark(self):
+        """Start of the timed region: summary() covers the samples from here
+        to stop()."""
+        self.first = len(self.lines)
+
+    def stop(self):
+        self.last = len(self.lines)
+        t0 = time.time()  # a short region: wait for the sample just after it
+        while (self.proc and len(self.lines) <= max(self.first, self.last)
+               and time.time() - t0 < 0.5):
+            time.sleep(0.01)
+        self.__exit__()
 
     def __enter__(self):
         try:
@@ -99,7 +126,7 @@ class Clocks:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
-        if self.proc:
+        if self.proc and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -111,7 +138,14 @@ class Clocks:
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
-        for l in self.lines:
+        last = len(self.lines) if self.last is None else self.last
+        lines = self.lines[self.first:last]
+        where = "during the timed region"
+        if not lines:  # a region shorter than the sampling period: the
+            # samples on either side of it
+            lines = self.lines[max(0, self.first - 1):last + 1]
+            where = "the samples just before and after the timed region"
+        for l in lines:
             p = [v.strip() for v in l.split(",")]
             if len(p) < 8:
                 continue
@@ -127,7 +161,8 @@ class Clocks:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
                     "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx),
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "sampled": where}
 
 
 def job_times(times, ws, device=None):
@@ -608,6 +643,7 @@ def run_engine(args):
     model = eng.upload(m.xyz, m.counts)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=local)
     out = np.zeros(len(K))
+    clk = Clocks(local).start()
     for _ in range(args.warmup):
         eng.pattern(model, m.rstep, m.nbins, m.species, K, mode=mode, out=out)
     # correctness guard: histogram totals must be the pair count
@@ -623,7 +659,8 @@ def run_engine(args):
     ev = [(torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     barrier()
-    with Clocks(local) as clk:
+    clk.mark()
+    try:
         for i in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()  # L2 flush (256 MB > 129 MB L2), not timed
@@ -646,6 +683,8 @@ def run_engine(args):
             mod2.free()
             e2e_s.append(time.perf_counter() - t0)
         h2d1, d2h1 = eng.traffic()
+    finally:
+        clk.stop()
     torch.cuda.synchronize()
     for a, b in ev:
         step_ms.append(a.elapsed_time(b))
