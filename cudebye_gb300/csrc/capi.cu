@@ -570,6 +570,7 @@ int dbx_destroy(dbx_ctx *c) {
   release(c, &c->hws.items);
   release(c, &c->hws.segs);
   release(c, &c->hws.tasks);
+  release(c, &c->hws.rows);
   release(c, &c->hws.partial);
   release(c, &c->hws.oor);
   if (c->batch.exec) cudaGraphExecDestroy(c->batch.exec);
