@@ -3,7 +3,8 @@
 second parity point beside the CPU oracle:
 
 * on the shipped Gamma-Al2O3 input it must write the six .debx files byte
-  for byte as shipped (the same digests the engine is held to), and
+  for byte as shipped (the same digests the engine is held to), on the
+  shipped UH3 input the shipped .debI and the engine's to 6 digits, and
 * on seeded synthetic models the engine's command line must write the same
   .debx files as the reference program, byte for byte, and a .debI that
   agrees to the format's print precision.
@@ -69,6 +70,30 @@ def test_reference_program_gamma_golden(refprog, golden_deb, golden, tmp_path):
         assert tt[int(i)] == b[0]
         # 6 significant digits on both sides: one unit of the last digit
         assert abs(ref_I[int(i)] - b[1]) <= 1.1e-5 * abs(b[1]), (i, ref_I[int(i)], b)
+
+
+def test_reference_program_uh3(refprog, golden_deb, golden, tmp_path):
+    """The other shipped input (UH3_7nm.deb, intensities only): the
+    reference program's .debI on this GPU, the shipped one and the
+    engine's command line agree to the format's 6 digits."""
+    ref_dir, eng_dir = tmp_path / "ref", tmp_path / "eng"
+    ref_dir.mkdir()
+    eng_dir.mkdir()
+    shutil.copy(golden_deb["UH3"], str(ref_dir / "UH3.deb"))
+    shutil.copy(golden_deb["UH3"], str(eng_dir / "UH3.deb"))
+    run_ref(refprog, str(ref_dir / "UH3.deb"))
+    r = subprocess.run([cd.CLI_PATH, str(eng_dir / "UH3.deb"), "--quiet"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    tt_r, I_r = read_debI(str(ref_dir / "UH3.debI"))
+    tt_e, I_e = read_debI(str(eng_dir / "UH3.debI"))
+    assert np.array_equal(tt_r, tt_e)
+    assert (np.abs(I_e - I_r) / np.abs(I_r)).max() <= 1.1e-5
+    g = golden["UH3"]["debI"]
+    assert len(tt_r) == g["lines"]
+    for i, want in g["sample"].items():
+        b = [float(v) for v in want.split("\t")]
+        assert abs(I_r[int(i)] - b[1]) <= 1.1e-5 * abs(b[1]), (i, I_r[int(i)], b)
 
 
 @pytest.mark.parametrize("case", ["spinel", "random3", "random1"])
