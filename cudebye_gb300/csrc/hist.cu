@@ -160,8 +160,10 @@ __device__ __forceinline__ int2 seg_item(const HistSeg &sg,
 
 // One warp = one tile pair (128 x 128 atoms). CTAs pull tasks from a global
 // counter in the order tasks[k].next (decreasing size, so the last tasks
-// to start are the short ones); task t's packed window goes to partial
-// slot t.
+// to start are the short ones), and warps pull the task's tile pairs from a
+// shared counter (warps progress unevenly under the issue scheduler; a
+// fixed round robin left the fast ones waiting at the task's end); task
+// t's packed window goes to partial slot t.
 __global__ void __launch_bounds__(kHistThreads, 1)
     hist_tiles_kernel(const int2 *__restrict__ items,
                       const HistTask *__restrict__ tasks, int ntasks,
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(kHistThreads, 1)
                       unsigned long long *__restrict__ oor_total,
                       int *__restrict__ task_counter) {
   extern __shared__ unsigned sh[];
-  __shared__ int s_task;
+  __shared__ int s_task, s_item;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (;;) {
     if (threadIdx.x == 0) {  // tasks are pulled largest first
@@ -183,6 +185,7 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     const HistTask tk = tasks[t];
     const HistSeg sg = segs[tk.seg];
     const int nw = (sg.wl + 1) >> 1;
+    if (threadIdx.x == 0) s_item = tk.item_begin;
     // window words, then 32 out-of-range words and 32 ignore words (one
     // each per lane), addressed as virtual bins 2 * word
     for (int i = threadIdx.x; i < nw + kSpareWords; i += kHistThreads)
@@ -209,8 +212,11 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     const unsigned pbase = base + olo, pwl = (unsigned)sg.own_len, pkb = kb + olo;
     unsigned long long *pgh = gh + olo;
     const unsigned pvo = vo - olo, pvi = vi - olo, pvend = vend - olo;
-    for (int it_i = tk.item_begin + warp; it_i < tk.item_end;
-         it_i += kHistThreads / 32) {
+    for (;;) {
+      int it_i = 0;
+      if (lane == 0) it_i = atomicAdd(&s_item, 1);
+      it_i = __shfl_sync(0xffffffffu, it_i, 0);
+      if (it_i >= tk.item_end) break;
       const int2 it = seg_item(sg, items, it_i);
       const bool diag = it.y < 0;
       const unsigned ix = (unsigned)it.x;
