@@ -44,7 +44,8 @@ struct BatchState {
 struct dbx_ctx {
   int device = 0;
   int num_sms = 0;
-  int hist_tasks = 0;  // histogram CTA tasks per launch
+  int hist_tasks = 0;  // histogram CTA tasks per launch of a batch
+  int hist_tasks_env = 0;  // DBX_HIST_TASKS, when set
   size_t budget = 0;  // 0 = no limit
   size_t used = 0;    // device bytes held
   cudaStream_t stream = nullptr;      // launch stream (own or caller's)
@@ -114,6 +115,17 @@ dbx::Model *find_model(dbx_ctx *c, int64_t id) {
 
 int64_t pitch_of(int64_t nbins) { return (nbins + 2 + 1) & ~int64_t(1); }
 
+// Histogram CTA tasks of one model's plan: 2 per SM when one window holds
+// the histogram (equal segments; every task boundary costs a window
+// zeroing and write-out: spinel_10nm 5.02 ms vs 5.06 at 4 per SM), 8 per
+// SM when several windows split it (segments of many sizes; finer tasks
+// fill the largest-first tail: Gamma sample 26.3 vs 26.7 ms).
+// DBX_HIST_TASKS overrides both.
+int model_tasks(const dbx_ctx *c, int64_t nbins) {
+  if (c->hist_tasks_env > 0) return c->hist_tasks_env;
+  return (nbins > dbx::hist_window_bins() ? 8 : 2) * c->num_sms;
+}
+
 // Histograms of all pairs, kept resident in the model. The work lists are
 // planned and uploaded once per (model, rstep, nbins) and reused. With
 // `launched` non-null the range check is left to the caller (who must call
@@ -152,7 +164,7 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
     m->plan_nbins = 0;
     if (nbins > dbx::hist_window_bins()) DBX_TRY(dbx::model_host_boxes(m, c->stream));
     DBX_TRY(dbx::hist_plan(*m, pairs, rstep, nbins, m->d_hist, pitch,
-                           c->hist_tasks, &m->plan_cache->plan));
+                           model_tasks(c, nbins), &m->plan_cache->plan));
     const size_t before = delta;
     Error e = dbx::hist_upload(m->plan_cache->plan, &m->plan_cache->lists,
                                c->stream, &delta);
@@ -550,7 +562,7 @@ int dbx_create(dbx_ctx **out, int device, size_t budget) {
   c->hist_tasks = 4 * c->num_sms;
   if (const char *v = getenv("DBX_HIST_TASKS")) {
     const int t = atoi(v);
-    if (t > 0) c->hist_tasks = t;
+    if (t > 0) c->hist_tasks = c->hist_tasks_env = t;
   }
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) !=
       cudaSuccess)
@@ -714,8 +726,8 @@ int dbx_pair_histogram(dbx_ctx *c, int64_t id, int row, int col, double rstep,
     if (e.code) return set_err(c, e);
   }
   e = dbx::hist_plan(*m, {make_int2(row, col)}, rstep, nbins,
-                     (unsigned long long *)c->tmp_hist.p, pitch, c->hist_tasks,
-                     &plan);
+                     (unsigned long long *)c->tmp_hist.p, pitch,
+                     model_tasks(c, nbins), &plan);
   if (e.code) return set_err(c, e);
   size_t delta = 0;
   c->tm.reset();

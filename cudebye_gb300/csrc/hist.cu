@@ -743,15 +743,32 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
   plan->tasks.clear();
   int64_t total = 0;
   for (int64_t p : plan->seg_pairs) total += p;
-  const double target =
-      std::max(1.0, (double)total / std::max(1, target_tasks));
-  for (size_t s = 0; s < plan->segs.size(); ++s) {
+  const size_t S = plan->segs.size();
+  // Task counts: each segment's share of target_tasks, rounded down, then
+  // the largest remainders get one more until the counts sum to exactly
+  // target_tasks (each count within [1, the segment's items]). The CTAs
+  // (one per SM) pull equal tasks, so a count a little above a multiple
+  // of the SM count would make a few CTAs run one task more than the rest:
+  // on spinel_10nm 457 tasks for 152 SMs took 6.34 ms, 608 took 5.06 ms.
+  std::vector<int64_t> ns(S);
+  std::vector<std::pair<double, size_t>> rem;
+  int64_t nsum = 0;
+  for (size_t s = 0; s < S; ++s) {
+    const int64_t items = plan->seg_items[s].y - plan->seg_items[s].x;
+    const double q = total > 0 ? (double)plan->seg_pairs[s] * target_tasks / total : 1.0;
+    ns[s] = std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)std::floor(q)));
+    nsum += ns[s];
+    if (ns[s] < items) rem.emplace_back(q - (double)ns[s], s);
+  }
+  std::stable_sort(rem.begin(), rem.end(),
+                   [](const auto &x, const auto &y) { return x.first > y.first; });
+  for (size_t k = 0; k < rem.size() && nsum < target_tasks; ++k, ++nsum)
+    ++ns[rem[k].second];
+  for (size_t s = 0; s < S; ++s) {
     HistSeg &sg = plan->segs[s];
     sg.task_begin = (int)plan->tasks.size();
     const int i0 = plan->seg_items[s].x, i1 = plan->seg_items[s].y;
-    const int64_t n_s = std::max<int64_t>(
-        1, std::min<int64_t>(i1 - i0,
-                             (int64_t)std::llround(plan->seg_pairs[s] / target)));
+    const int64_t n_s = ns[s];
     if (sg.shape != kSegList) {
       for (int64_t k = 0; k < n_s; ++k) {
         const int b = (int)(i0 + (i1 - i0) * k / n_s);
