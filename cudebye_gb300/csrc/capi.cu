@@ -557,8 +557,9 @@ int dbx_create(dbx_ctx **out, int device, size_t budget) {
   if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount,
                              device) != cudaSuccess)
     return DBX_ERR_CUDA;
-  // Tasks per histogram launch: 4 per SM by default. DBX_HIST_TASKS
-  // overrides it (tuning; fewer tasks also means more counts per task).
+  // Histogram tasks: a batch plan starts its autotuning from 4 per SM, a
+  // single model's plan takes model_tasks(). DBX_HIST_TASKS fixes both
+  // (tuning; fewer tasks also means more counts per task).
   c->hist_tasks = 4 * c->num_sms;
   if (const char *v = getenv("DBX_HIST_TASKS")) {
     const int t = atoi(v);
