@@ -300,10 +300,13 @@ __global__ void hist_reduce_kernel(const unsigned *__restrict__ partial,
   }
 }
 
-// Zero the output histograms of a plan (one block per row).
+// Zero the output histograms of a plan (row blockIdx.x, split over
+// gridDim.y blocks).
 __global__ void hist_zero_kernel(const HistRow *__restrict__ rows) {
   const HistRow r = rows[blockIdx.x];
-  for (long long i = threadIdx.x; i < r.len; i += blockDim.x) r.out[i] = 0ull;
+  for (long long i = blockIdx.y * (long long)blockDim.x + threadIdx.x; i < r.len;
+       i += (long long)gridDim.y * blockDim.x)
+    r.out[i] = 0ull;
 }
 
 // One thread per pair (i of the row block, j of the column block), blocks of
@@ -906,9 +909,11 @@ Error hist_launch(const HistPlan &plan, const HistWorkspace &lists,
   for (const HistSeg &s : plan.segs) max_wl = std::max(max_wl, s.wl);
   const int words = (max_wl + 1) / 2;
   DBX_TRY(hist_scratch(plan, ws, ws_bytes_delta));
-  if (!plan.rows.empty())
-    hist_zero_kernel<<<(unsigned)plan.rows.size(), 256, 0, stream>>>(
+  if (!plan.rows.empty()) {  // a few rows (one model): several blocks each
+    const unsigned per_row = plan.rows.size() < 64 ? 16u : 1u;
+    hist_zero_kernel<<<dim3((unsigned)plan.rows.size(), per_row), 256, 0, stream>>>(
         (const HistRow *)lists.rows.p);
+  }
   // oor counter and the task counter share one 16-byte buffer
   DBX_CUDA_TRY(cudaMemsetAsync(ws->oor.p, 0, 2 * sizeof(unsigned long long), stream));
   if (ntasks == 0) return ok();
