@@ -13,10 +13,16 @@ Expected", cuDebye-v15.cu:372,:396) per pattern.
 ``value``: device time per step (CUDA events on the engine's launch stream,
 model resident in HBM, L2 flushed between steps). ``e2e``: the same metric
 through the C ABI with host buffers (upload from host coordinates, pattern,
-intensities read back, model freed) per step. ``--impl reference`` times
-the reference's arithmetic on the host cores (the C/OpenMP oracle; the
-reference itself has no CPU path) on a bounded sample of the workload.
-Multi-GPU: independent replicas per rank (the path needs no exchange).
+intensities read back, model freed) per step. ``cpu_baseline``: the oracle
+(C/OpenMP) on all host cores over one full pattern. ``--impl reference``
+times the reference's arithmetic on the host cores (the C/OpenMP oracle;
+the reference program itself has no CPU path), one full pattern per step,
+and runs the reference program once on the GPU beside it. Further legs:
+``plain_small`` (5,000 atoms), ``batch256`` (the 256-model mix, batched vs
+the plain FP32 GPU form), ``precision`` (20,000 q), ``file_io``,
+``serving`` (Poisson arrivals of fresh requests); the benchmark spec sums them
+up last on the line. Multi-GPU: independent replicas per rank (the path
+needs no exchange).
 """
 import argparse
 import json
@@ -201,47 +207,56 @@ def workload():
     return WORKLOADS[WORKLOAD](lattice)
 
 
-def cpu_baseline(m, K, budget_s=12.0, threads=0):
-    """Oracle timing on the host cores on a bounded sample: every s-th row
-    atom of each pair block for the histogram and every t-th q point for the
-    Debye sum, extrapolated to one full pattern."""
+def cpu_model():
+    """The host CPU's model name (lscpu "Model name", else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True,
+                             timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def oracle_pattern(m, K, threads=0):
+    """One full pattern by the oracle on the host cores (C/OpenMP): every
+    pair histogram of every atom (cuDebye-v15.cu:88-146) and the FP64 Debye
+    sum at every q (:493-538). Returns (seconds, histogram seconds)."""
     from oracle import pyoracle as orc
     orc.lib()
-    starts = np.concatenate([[0], np.cumsum(m.counts)[:-1]])
-    stride = 8
     t0 = time.perf_counter()
-    sampled = 0
-    hists = []
-    for r in range(len(m.counts)):
-        for c in range(r, len(m.counts)):
-            h, _ = orc.block_histogram(m.xyz, starts[r], m.counts[r],
-                                       starts[c], m.counts[c], r == c, m.rstep,
-                                       m.nbins, threads, stride)
-            hists.append(h)
-            n = m.counts[r]
-            rows = len(range(0, n, stride))
-            sampled += (sum(i + 1 for i in range(0, n, stride)) if r == c
-                        else rows * m.counts[c])
-    t_hist = time.perf_counter() - t0
-    hist_rate = sampled / t_hist
-    # Debye: full histograms are needed for a representative bin count; the
-    # sampled histograms have the same support, so time on them.
-    qs = 8
-    t0 = time.perf_counter()
-    orc.intensity(K, hists, m.species, m.rstep, threads=threads, q_stride=qs)
-    t_deb = (time.perf_counter() - t0) * qs
-    t_pattern = m.pairs / hist_rate + t_deb
+    hists, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins,
+                                      threads)
+    t1 = time.perf_counter()
+    orc.intensity(K, hists, m.species, m.rstep, threads=threads)
+    t2 = time.perf_counter()
+    if bad:
+        raise RuntimeError("oracle: %d distances beyond rmax" % bad)
+    return t2 - t0, t1 - t0
+
+
+def cpu_baseline(m, K, threads=0):
+    """The oracle timed on one full pattern of the workload (no sampling,
+    no extrapolation) on all host cores."""
+    t, th = oracle_pattern(m, K, threads)
     cores = threads or os.cpu_count()
-    return {
-        "value": m.pairs / t_pattern / 1e9, "unit": METRIC, "cores": cores,
-        "kind": "port",
-        "sample": "oracle (C/OpenMP, %d threads): histogram of every %dth row "
-                  "atom (%.3g pairs, %.2f s) + FP64 Debye sum at every %dth q "
-                  "(%.2f s), extrapolated to one full pattern (%.1f s)"
-                  % (cores, stride, sampled, t_hist, qs, t_deb / qs, t_pattern),
-        "pattern_s": t_pattern, "hist_pairs_per_s": hist_rate,
-        "debye_s": t_deb,
-    }
+    return {"value": m.pairs / t / 1e9, "unit": METRIC, "cores": cores,
+            "cpu_model": cpu_model(), "kind": "port",
+            "sample": "one full pattern of %s: oracle (C/OpenMP, %d threads), "
+                      "all %d pair histograms (%.2f s) + FP64 Debye sum at all "
+                      "%d q (%.2f s)" % (m.label, cores, len(m.counts) *
+                                         (len(m.counts) + 1) // 2, th,
+                                         len(K), t - th),
+            "pattern_s": t}
 
 
 def batch_bench(eng, steps=5, seed=3, nmodels=256, plain_models=None):
@@ -274,9 +289,10 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, plain_models=None):
         # FP64 direct sum of its resident histograms (dbx_pattern_errors)
         per = eng.pattern_errors(hs, 1e-3, nb, sp, K, I, q_stride=10).tolist()
         worst = max(per)
-        # plain form over a subset (it is slow), scaled per pattern
-        sub = list(range(len(mods))) if plain_models is None else \
-            list(range(min(plain_models, len(mods))))
+        # the plain form over the whole mix (a smaller count only for quick
+        # runs: every `step`-th model, scaled per pattern)
+        step = 1 if not plain_models else max(1, len(mods) // plain_models)
+        sub = list(range(0, len(mods), step))
         sp_sub = [s for i in sub for s in mods[i].species]
         t0 = time.perf_counter()
         eng.patterns([hs[i] for i in sub], 1e-3, [nb[i] for i in sub], sp_sub,
@@ -299,7 +315,9 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, plain_models=None):
                          "reference's arithmetic; tests hold it within 1e-11 "
                          "of the CPU FP64 oracle",
         "timing": "host wall clock around dbx_patterns (H2D species/K, graph "
-                  "replay, D2H of all intensities), median of %d passes" % steps,
+                  "replay, D2H of all intensities), median of %d passes; "
+                  "plain form: one pass over %d of %d models"
+                  % (steps, len(sub), len(mods)),
     }
 
 
@@ -422,88 +440,154 @@ def io_bench(eng, nfiles=16, seed=8):
     return out
 
 
-def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, pool=32,
-                  seed=4, budget_gib=16):
+class RequestFeed:
+    """Fresh serving requests from spawned worker processes
+    (lattice.request_worker): each request has its own geometry and its own
+    2theta grid, made off the submitting thread so that the arrival
+    schedule is kept."""
+
+    def __init__(self, seed, workers=None):
+        import multiprocessing as mp
+        from cudebye_gb300 import lattice
+        self.lattice = lattice
+        n = workers or max(2, min(6, (os.cpu_count() or 4) // 2))
+        ctx = mp.get_context("spawn")
+        self.q = ctx.Queue(maxsize=256)
+        self.stop_ev = ctx.Event()
+        self.procs = [ctx.Process(target=lattice.request_worker,
+                                  args=(seed * 1000 + i, self.q, self.stop_ev),
+                                  daemon=True) for i in range(n)]
+        for p in self.procs:
+            p.start()
+        self.waited_s = 0.0  # time the arrival loop waited for a request
+
+    def get(self):
+        import queue
+        t0 = time.perf_counter()
+        while True:
+            try:
+                item = self.q.get(timeout=5.0)
+                break
+            except queue.Empty:
+                if not any(p.is_alive() for p in self.procs):
+                    raise RuntimeError("request workers exited")
+        self.waited_s += time.perf_counter() - t0
+        return self.lattice.model_from_item(item)
+
+    def close(self):
+        import queue
+        self.stop_ev.set()
+        t0 = time.perf_counter()
+        while any(p.is_alive() for p in self.procs) and time.perf_counter() - t0 < 20:
+            try:
+                while True:
+                    self.q.get_nowait()
+            except queue.Empty:
+                pass
+            for p in self.procs:
+                p.join(timeout=0.05)
+        for p in self.procs:
+            if p.is_alive():
+                p.terminate()
+
+
+def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, seed=4,
+                  budget_gib=16):
     """The serving form: Poisson arrivals at each rate for `seconds`; each
-    request is a spherical lattice model of 1,000-200,000 atoms
-    (log-uniform, 1-4 species) with its own 2theta grid of 2,000-20,000
-    points, or, with probability 0.2, a re-scoring of a resident model with
-    new B factors. Latency = submit to result, measured by the server.
-    Requests are drawn from a pool of `pool` seeded models (generated once).
-    The server admits by HBM footprint within `budget_gib`, evicting idle
-    resident models; a re-score of a model evicted meanwhile fails with
-    DBX_ERR_MODEL and is counted, not timed."""
+    new request is a fresh spherical lattice model of 1,000-200,000 atoms
+    (log-uniform, 1-4 species, random orientation and jitter) with its own
+    2theta grid of 2,000-20,000 points, or, with probability 0.2, a
+    re-scoring of a resident model with new B factors. Latency = submit to
+    result, measured by the server. The server admits by HBM footprint
+    within `budget_gib`, evicting idle resident models; a re-score of a
+    model evicted meanwhile fails with DBX_ERR_MODEL and is counted, not
+    timed."""
     import concurrent.futures as cf
     import cudebye_gb300 as cd
     from cudebye_gb300 import lattice
     rng = np.random.default_rng(seed)
-    models = [lattice.serving_request(rng) for _ in range(pool)]
-    grids = [m.k_grid()[1] for m in models]
+    feed = RequestFeed(seed)
     out = []
-    with cd.Server(0, hbm_budget=budget_gib << 30) as srv:
-        # warm-up: one pass over a few pool models
-        for m, K in list(zip(models, grids))[:4]:
-            srv.wait(srv.submit(m.species, m.rstep, m.nbins, K, xyz=m.xyz,
-                                counts=m.counts), len(K))
-        for rate in rates:
-            lat, done_t, resident, failed = [], [], [], []
-            lock = threading.Lock()
-            ex = cf.ThreadPoolExecutor(max_workers=64)
+    try:
+        with cd.Server(0, hbm_budget=budget_gib << 30) as srv:
+            for _ in range(4):  # warm-up
+                m = feed.get()
+                K = m.k_grid()[1]
+                srv.wait(srv.submit(m.species, m.rstep, m.nbins, K, xyz=m.xyz,
+                                    counts=m.counts), len(K))
+            for rate in rates:
+                lat, done_t, resident, failed = [], [], [], []
+                lock = threading.Lock()
+                ex = cf.ThreadPoolExecutor(max_workers=64)
+                atoms = []
 
-            def waiter(t, nq, pi, t0):
-                try:
-                    I, mid, ms = srv.wait(t, nq)
-                except cd.DebyeError as err:  # re-score of an evicted model
+                def waiter(t, nq, rec, t0):
+                    try:
+                        I, mid, ms = srv.wait(t, nq)
+                    except cd.DebyeError as err:  # re-score of an evicted model
+                        with lock:
+                            failed.append(err.code)
+                        return
                     with lock:
-                        failed.append(err.code)
-                    return
-                with lock:
-                    lat.append(ms)
-                    done_t.append(time.perf_counter() - t0)
-                    if pi is not None:
-                        resident.append((mid, pi))
+                        lat.append(ms)
+                        done_t.append(time.perf_counter() - t0)
+                        if rec is not None:
+                            resident.append((mid,) + rec)
 
-            t0 = time.perf_counter()
-            tnext, k, futs, nsub, nres = 0.0, 0, [], 0, 0
-            while tnext < seconds:
-                now = time.perf_counter() - t0
-                if now < tnext:
-                    time.sleep(min(tnext - now, 0.002))
-                    continue
-                with lock:
-                    can = bool(resident)
-                if can and rng.random() < 0.2:
+                waited0 = feed.waited_s
+                t0 = time.perf_counter()
+                tnext, futs, nsub, nres, late = 0.0, [], 0, 0, 0.0
+                while tnext < seconds:
                     with lock:
-                        mid, pi = resident[int(rng.integers(len(resident)))]
-                    m = models[pi]
-                    sp = [lattice.species(n, s.occ, float(rng.uniform(0.2, 1.5)))
-                          for n, s in zip(m.names, m.species)]
-                    t = srv.submit(sp, m.rstep, m.nbins, grids[pi], model=mid)
-                    futs.append(ex.submit(waiter, t, len(grids[pi]), None, t0))
-                    nres += 1
-                else:
-                    pi = k % pool
-                    k += 1
-                    m = models[pi]
-                    t = srv.submit(m.species, m.rstep, m.nbins, grids[pi],
-                                   xyz=m.xyz, counts=m.counts)
-                    futs.append(ex.submit(waiter, t, len(grids[pi]), pi, t0))
-                nsub += 1
-                tnext += rng.exponential(1.0 / rate)
-            for f in futs:
-                f.result()
-            ex.shutdown()
-            span = max(done_t) if done_t else seconds
-            out.append({"rate": rate, "submitted": nsub, "rescored": nres,
-                        "failed_evicted": len(failed),
-                        "patterns_per_s": len(lat) / span,
-                        "p50_ms": float(np.percentile(lat, 50)),
-                        "p99_ms": float(np.percentile(lat, 99))})
-        st = srv.stats()
+                        can = bool(resident)
+                    if can and rng.random() < 0.2:
+                        with lock:
+                            mid, names, rstep, nbins, K = resident[
+                                int(rng.integers(len(resident)))]
+                        sp = [lattice.species(n, 1.0, float(rng.uniform(0.2, 1.5)))
+                              for n in names]
+                        req = (sp, rstep, nbins, K, dict(model=mid), None)
+                    else:
+                        m = feed.get()
+                        K = m.k_grid()[1]
+                        req = (m.species, m.rstep, m.nbins, K,
+                               dict(xyz=m.xyz, counts=m.counts),
+                               (m.names, m.rstep, m.nbins, K))
+                        atoms.append(m.natoms)
+                    now = time.perf_counter() - t0
+                    if now < tnext:
+                        time.sleep(tnext - now)
+                    else:
+                        late = max(late, now - tnext)
+                    sp, rstep, nbins, K, kw, rec = req
+                    t = srv.submit(sp, rstep, nbins, K, **kw)
+                    futs.append(ex.submit(waiter, t, len(K), rec, t0))
+                    if rec is None:
+                        nres += 1
+                    nsub += 1
+                    tnext += rng.exponential(1.0 / rate)
+                for f in futs:
+                    f.result()
+                ex.shutdown()
+                span = max(done_t) if done_t else seconds
+                out.append({"rate": rate, "submitted": nsub, "rescored": nres,
+                            "failed_evicted": len(failed),
+                            "patterns_per_s": len(lat) / span,
+                            "p50_ms": float(np.percentile(lat, 50)),
+                            "p99_ms": float(np.percentile(lat, 99)),
+                            "mean_atoms": float(np.mean(atoms)) if atoms else 0.0,
+                            "max_arrival_lag_s": late,
+                            "feed_wait_s": feed.waited_s - waited0})
+            st = srv.stats()
+    finally:
+        feed.close()
     sat = max([o["rate"] for o in out
                if o["patterns_per_s"] >= 0.9 * o["rate"]] or [0])
     return {"rates": out, "saturation_req_per_s": sat,
-            "seconds_per_rate": seconds, "pool_models": pool,
+            "seconds_per_rate": seconds,
+            "requests": "fresh geometry and 2theta grid per new request "
+                        "(lattice.RequestStream in %d spawned workers)"
+                        % len(feed.procs),
             "hbm_budget_gib": budget_gib,
             "rounds": st["rounds"], "evictions": st["evictions"],
             "timing": "host clock; latency measured by the server from "
@@ -582,44 +666,126 @@ def reference_program_batch(step=16, seed=3):
             "patterns_per_s_process": len(runs) / wall}
 
 
+def run_config(m, K):
+    """The `config` of both arms' lines (the same keys and values)."""
+    return {"workload": m.label, "atoms": m.natoms,
+            "species": len(m.counts),
+            "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
+            "bins": m.nbins, "rstep": m.rstep, "q_points": len(K),
+            "binned_pairs": m.pairs,
+            "l2": "engine arm: L2 flushed between steps (256 MB write); "
+                  "reference arm: host caches not flushed"}
+
+
 def run_reference(args):
+    """The reference arm: the reference's arithmetic (the C/OpenMP oracle;
+    the reference program has no CPU path) on all host cores, one full
+    pattern per step: every pair histogram and the FP64 Debye sum at every
+    q. Rank 0 only."""
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
     m = workload()
     tt, K = m.k_grid()
-    for _ in range(args.warmup):  # untimed samples: caches, page faults
-        cpu_baseline(m, K, threads=0)
-    vals = []
+    for _ in range(args.warmup):  # untimed: page faults, thread start-up
+        oracle_pattern(m, K)
+    ts, th = [], []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(m, K, threads=0))
+        t, h = oracle_pattern(m, K)
+        ts.append(t)
+        th.append(h)
     wall = time.perf_counter() - t0
-    v = float(np.median([b["value"] for b in vals]))
-    b = vals[-1]
+    t_step = float(np.mean(ts))
+    v = m.pairs / t_step / 1e9
+    cores = os.cpu_count()
     line = {
         "metric": METRIC, "value": v, "unit": METRIC, "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": b["pattern_s"] * 1e3, "higher_is_better": True,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded spinel-like nanoparticle)",
-        "config": {"workload": m.label, "atoms": m.natoms,
-                   "species": len(m.counts), "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
-                   "bins": m.nbins, "rstep": m.rstep, "q_points": len(K),
-                   "binned_pairs": m.pairs,
-                   "parallelism": "host threads of rank 0",
-                   "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": v, "unit": METRIC, "cores": b["cores"],
-                         "kind": "port", "sample": b["sample"]},
+        "config": run_config(m, K),
+        "debye_mode": "fp64",
+        "parallelism": "%d host threads of rank 0" % cores,
+        "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores,
+                         "cpu_model": cpu_model(), "kind": "port",
+                         "sample": "every step one full pattern (no sampling): "
+                                   "oracle histograms %.2f s + FP64 Debye sum "
+                                   "%.2f s (means)" % (np.mean(th),
+                                                       t_step - np.mean(th))},
         "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "wall_s": wall,
+        "timed_region_s": wall,
     }
     if not args.no_refprog:
         line["reference_program_gpu"] = reference_program(m)
         line["reference_program_gpu_batch256"] = reference_program_batch()
     print(json.dumps(line))
     return 0
+
+
+def pattern_leg(eng, stream, m, K, mode, steps, warmup, flush, clk=None,
+                barrier=None):
+    """Full patterns of one resident model: `steps` device-timed passes (CUDA
+    events on the engine's stream, L2 flushed by `flush` before each), then
+    `steps` end-to-end passes through the C ABI from host coordinates
+    (upload incl. sort and plan, pattern, intensities read back, model
+    freed). The histogram total is checked against the pair count."""
+    import torch
+    import cudebye_gb300 as cd
+    eng.set_stream(stream.cuda_stream)
+    model = eng.upload(m.xyz, m.counts)
+    out = np.zeros(len(K))
+    try:
+        for _ in range(warmup):
+            eng.pattern(model, m.rstep, m.nbins, m.species, K, mode=mode, out=out)
+        h = eng.histogram(model, m.rstep, m.nbins)
+        assert int(h.sum()) == m.pairs, "histogram total != binned pairs"
+        phase = {k: [] for k in cd.TIMERS}
+        ev = [(torch.cuda.Event(enable_timing=True),
+               torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        if barrier:
+            barrier()
+        torch.cuda.synchronize()
+        if clk:
+            clk.mark()
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()  # L2 flush (256 MB > 129 MB L2), not timed
+            ev[i][0].record(stream)
+            eng.pattern(model, m.rstep, m.nbins, m.species, K, mode=mode, out=out)
+            ev[i][1].record(stream)
+            for k, v in eng.timing().items():
+                phase[k].append(v)
+        if barrier:
+            barrier()
+        torch.cuda.synchronize()
+        h2d0, d2h0 = eng.traffic()
+        eng.set_stream(None)
+        e2e_s = []
+        for i in range(steps):
+            t0 = time.perf_counter()
+            mod2 = eng.upload(m.xyz, m.counts)
+            eng.pattern(mod2, m.rstep, m.nbins, m.species, K, mode=mode, out=out)
+            mod2.free()
+            e2e_s.append(time.perf_counter() - t0)
+        h2d1, d2h1 = eng.traffic()
+        if clk:
+            clk.stop()
+        torch.cuda.synchronize()
+    finally:
+        model.free()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    return {"t_step": float(np.mean(step_ms)) / 1e3,
+            "t_e2e": float(np.mean(e2e_s)),
+            "phase_ms": {k: float(np.mean(v)) for k, v in phase.items()},
+            "h2d": (h2d1 - h2d0) // steps, "d2h": (d2h1 - d2h0) // steps}
+
+
+def sig(v, n=4):
+    """v rounded to n significant digits (compact summary values)."""
+    return float("%.*g" % (n, v)) if isinstance(v, float) else v
 
 
 def run_engine(args):
@@ -637,66 +803,26 @@ def run_engine(args):
     tt, K = m.k_grid()
     eng = cd.Engine(local)
     stream = torch.cuda.Stream(device=local)
-    eng.set_stream(stream.cuda_stream)
     eng.set_timing(True)
     mode = args.mode
-    model = eng.upload(m.xyz, m.counts)
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=local)
-    out = np.zeros(len(K))
     clk = Clocks(local).start()
-    for _ in range(args.warmup):
-        eng.pattern(model, m.rstep, m.nbins, m.species, K, mode=mode, out=out)
-    # correctness guard: histogram totals must be the pair count
-    h = eng.histogram(model, m.rstep, m.nbins)
-    assert int(h.sum()) == m.pairs, "histogram total != binned pairs"
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    step_ms, phase = [], {k: [] for k in cd.TIMERS}
-    ev = [(torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier()
-    clk.mark()
-    try:
-        for i in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()  # L2 flush (256 MB > 129 MB L2), not timed
-            ev[i][0].record(stream)
-            eng.pattern(model, m.rstep, m.nbins, m.species, K, mode=mode,
-                        out=out)
-            ev[i][1].record(stream)
-            for k, v in eng.timing().items():
-                phase[k].append(v)
-        barrier()
-        # end-to-end through the C ABI with host buffers
-        h2d0, d2h0 = eng.traffic()
-        eng.set_stream(None)
-        e2e_s = []
-        for i in range(args.steps):
-            t0 = time.perf_counter()
-            mod2 = eng.upload(m.xyz, m.counts)
-            eng.pattern(mod2, m.rstep, m.nbins, m.species, K, mode=mode,
-                        out=out)
-            mod2.free()
-            e2e_s.append(time.perf_counter() - t0)
-        h2d1, d2h1 = eng.traffic()
-    finally:
-        clk.stop()
-    torch.cuda.synchronize()
-    for a, b in ev:
-        step_ms.append(a.elapsed_time(b))
-    t_step = float(np.mean(step_ms)) / 1e3
-    t_e2e = float(np.mean(e2e_s))
-    t_step, t_e2e = job_times([t_step, t_e2e], ws, device=local)
+    lead = pattern_leg(eng, stream, m, K, mode, args.steps, args.warmup, flush,
+                       clk=clk, barrier=barrier)
+    t_step, t_e2e = job_times([lead["t_step"], lead["t_e2e"]], ws, device=local)
     if rank != 0:
         eng.close()
         return 0
     pk, pk_kind = peaks()
     clocks = clk.summary()
-    ph = {k: float(np.mean(v)) for k, v in phase.items()}
+    ph = lead["phase_ms"]
     npair_types = len(m.counts) * (len(m.counts) + 1) // 2
     total_pairs = m.pairs * ws
     value = total_pairs / t_step / 1e9
@@ -705,11 +831,11 @@ def run_engine(args):
     sm_mhz = clocks["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)
     # FP32-pipe bound of the reference's exact bin formula: 16 FP32
     # operations per pair (3 sub, 3 mul, 2 add, square root as estimate + 4
-    # correction ops, 1 mul, 2 for roundf), 152 SMs x 128 FP32 lanes per
-    # clock. Packed FP32x2 instructions do two of these per lane and issue
-    # slot, so a kernel can exceed this bound.
+    # correction ops, 1 mul, 2 for roundf), SMs x 128 FP32 lanes per clock.
+    # Packed FP32x2 instructions do two of these per lane and issue slot, so
+    # a kernel can exceed this bound.
     ops = 16
-    peak = 152 * 128 * sm_mhz * 1e6 / ops / 1e9
+    peak = nsm * 128 * sm_mhz * 1e6 / ops / 1e9
     ach = m.pairs / (ph["hist"] / 1e3) / 1e9
     roof = {"kernel": "hist_tiles_kernel", "bound": "alu",
             "achieved": ach, "peak": peak, "unit": "Gpair/s",
@@ -717,8 +843,8 @@ def run_engine(args):
             "traffic": measured_traffic("hist_tiles_kernel", m.label),
             "traffic_unit": "DRAM bytes per launch (ncu)",
             "algorithmic_bytes": 16 * m.natoms + 8 * m.nbins * npair_types,
-            "peak_basis": "FP32 pipe, %d ops/pair at %.0f MHz (median "
-                          "sampled SM clock)" % (ops, sm_mhz)}
+            "peak_basis": "FP32 pipe, %d ops/pair, %d SMs at %.0f MHz (median "
+                          "sampled SM clock)" % (ops, nsm, sm_mhz)}
     # the same launch against the measured HBM copy bandwidth: the kernel
     # moves O(atoms + bins) bytes for O(atoms^2) work, so it is far from it
     alg_gbs = roof["algorithmic_bytes"] / (ph["hist"] / 1e3) / 1e9
@@ -753,17 +879,14 @@ def run_engine(args):
         "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded spinel-like nanoparticle)",
-        "config": {"workload": m.label, "atoms": m.natoms,
-                   "species": len(m.counts), "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
-                   "bins": m.nbins, "rstep": m.rstep, "q_points": len(K),
-                   "binned_pairs": m.pairs, "debye_mode": mode,
-                   "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "flushed between steps (256 MB write)"},
+        "config": run_config(m, K),
+        "debye_mode": mode,
+        "parallelism": "replicas" if ws > 1 else "single",
         "patterns_per_s": ws / t_step,
         "phase_ms": ph,
         "e2e": {"value": total_pairs / t_e2e / 1e9, "unit": METRIC,
-                "h2d_bytes_per_step": (h2d1 - h2d0) // args.steps,
-                "d2h_bytes_per_step": (d2h1 - d2h0) // args.steps,
+                "h2d_bytes_per_step": lead["h2d"],
+                "d2h_bytes_per_step": lead["d2h"],
                 "ms_per_step": t_e2e * 1e3},
         "gpu_launches": args.steps * launches_per_pattern(mode, npair_types),
         "roofline": roof,
@@ -772,18 +895,60 @@ def run_engine(args):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(m, K).items()
-                                if k in ("value", "unit", "cores", "kind",
-                                         "sample")}
+                                if k != "pattern_s"}
+    if not args.no_small:  # the small-input regime: plain_small, 5,000 atoms
+        from cudebye_gb300 import lattice
+        ms = WORKLOADS["plain_small"](lattice)
+        _, Ks = ms.k_grid()
+        leg = pattern_leg(eng, stream, ms, Ks, mode, args.steps, args.warmup,
+                          flush)
+        small = {"config": run_config(ms, Ks),
+                 "value": ms.pairs / leg["t_step"] / 1e9, "unit": METRIC,
+                 "ms_per_step": leg["t_step"] * 1e3,
+                 "patterns_per_s": 1.0 / leg["t_step"],
+                 "phase_ms": leg["phase_ms"],
+                 "e2e": {"value": ms.pairs / leg["t_e2e"] / 1e9, "unit": METRIC,
+                         "h2d_bytes_per_step": leg["h2d"],
+                         "d2h_bytes_per_step": leg["d2h"],
+                         "ms_per_step": leg["t_e2e"] * 1e3}}
+        if not args.no_cpu:
+            small["cpu_baseline"] = {k: v for k, v in cpu_baseline(ms, Ks).items()
+                                     if k != "pattern_s"}
+        line["plain_small"] = small
     if not args.no_batch:
         line["batch256"] = batch_bench(eng, plain_models=args.plain_models)
     if not args.no_io:
         line["file_io"] = io_bench(eng)
     if not args.no_precision:
         line["precision"] = precision_bench(eng)
-    model.free()
     eng.close()
     if not args.no_serve:
-        line["serving"] = serving_bench(seconds=args.serve_seconds)
+        rates = [int(r) for r in args.serve_rates.split(",")]
+        line["serving"] = serving_bench(rates=rates, seconds=args.serve_seconds)
+    # The benchmark spec's figures, last on the line: batched vs plain patterns/s
+    # on the 256-model mix with the worst error, p50/p99 under the serving
+    # load, and the small-input leg.
+    ns = {}
+    if "batch256" in line:
+        b = line["batch256"]
+        ns["batch256"] = {k: sig(b[k]) for k in (
+            "patterns_per_s_batched", "patterns_per_s_plain",
+            "speedup_batched_vs_plain", "max_rel_err_vs_fp64",
+            "patterns_over_1e-6", "err_models_checked")}
+    if "serving" in line:
+        r = [o for o in line["serving"]["rates"] if o["rate"] == 200] or \
+            line["serving"]["rates"][-1:]
+        if r:
+            ns["serving"] = {k: sig(r[0][k]) for k in (
+                "rate", "submitted", "patterns_per_s", "p50_ms", "p99_ms")}
+            ns["serving"]["saturation_req_per_s"] = \
+                line["serving"]["saturation_req_per_s"]
+    if "plain_small" in line:
+        ns["plain_small"] = {"value": sig(line["plain_small"]["value"]),
+                             "e2e": sig(line["plain_small"]["e2e"]["value"])}
+    ns["headline"] = {"value": sig(value), "e2e": sig(line["e2e"]["value"]),
+                      "hist_frac": sig(roof["frac"], 3)}
+    line["north_star"] = ns
     print(json.dumps(line))
     return 0
 
@@ -801,8 +966,13 @@ def main():
                     choices=sorted(WORKLOADS))
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 256-model batched comparison")
-    ap.add_argument("--plain-models", type=int, default=64,
-                    help="models of the batch timed in the plain form")
+    ap.add_argument("--plain-models", type=int, default=0,
+                    help="models of the batch timed in the plain form "
+                         "(0: all)")
+    ap.add_argument("--no-small", action="store_true",
+                    help="skip the plain_small (5,000 atoms) leg")
+    ap.add_argument("--serve-rates", default="5,20,50,100,200,400,800",
+                    help="arrival rates of the serving run (req/s)")
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the serving run")
     ap.add_argument("--no-io", action="store_true",

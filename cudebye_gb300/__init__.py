@@ -46,7 +46,8 @@ MODES = {"tc": 0, "fp64": 1, "fp32": 2, "plain": 3, "tc3": 4}
 EXPORTS = (
     "dbx_create", "dbx_destroy", "dbx_strerror", "dbx_last_error",
     "dbx_device_bytes", "dbx_model_upload", "dbx_model_free",
-    "dbx_pair_histogram", "dbx_histogram", "dbx_channels", "dbx_reduce_check",
+    "dbx_pair_histogram", "dbx_pair_histogram_plain", "dbx_histogram",
+    "dbx_channels", "dbx_reduce_check",
     "dbx_k_grid", "dbx_atomic_prop", "dbx_intensity", "dbx_pattern",
     "dbx_set_stream", "dbx_set_timing", "dbx_get_timing", "dbx_get_traffic",
     "dbx_run_deb", "dbx_pair_histogram_noalloc", "dbx_patterns",
@@ -138,6 +139,9 @@ def load_library(path=None):
         "dbx_pair_histogram": (ctypes.c_int, [c_p, ctypes.c_int64, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_double,
                                               ctypes.c_int64, i64p]),
+        "dbx_pair_histogram_plain": (ctypes.c_int, [
+            c_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+            ctypes.c_int64, i64p]),
         "dbx_histogram": (ctypes.c_int, [c_p, ctypes.c_int64, ctypes.c_double,
                                          ctypes.c_int64, i64p]),
         "dbx_channels": (ctypes.c_int64, [ctypes.c_double, ctypes.c_double]),
@@ -434,6 +438,15 @@ class Engine:
         """int64 histogram of species pair (row, col) (splitCalcDist)."""
         out = np.zeros(nbins, dtype=np.int64)
         self._check(self.lib.dbx_pair_histogram(
+            self.ctx, model.id, row, col, rstep, nbins,
+            _ptr(out, ctypes.c_int64)))
+        return out
+
+    def split_calc_dist_plain(self, model, row, col, rstep, nbins):
+        """The same histogram from the plain unbatched FP32 GPU form (one
+        thread per pair, global atomics; dbx_pair_histogram_plain)."""
+        out = np.zeros(nbins, dtype=np.int64)
+        self._check(self.lib.dbx_pair_histogram_plain(
             self.ctx, model.id, row, col, rstep, nbins,
             _ptr(out, ctypes.c_int64)))
         return out

@@ -742,6 +742,31 @@ int dbx_pair_histogram(dbx_ctx *c, int64_t id, int row, int col, double rstep,
                               pitch, nbins, 1, out));
 }
 
+int dbx_pair_histogram_plain(dbx_ctx *c, int64_t id, int row, int col,
+                             double rstep, int64_t nbins, int64_t *out) {
+  if (!c || !out || !(rstep > 0) || nbins < 1) return DBX_ERR_ARG;
+  cudaSetDevice(c->device);
+  dbx::Model *m = find_model(c, id);
+  if (!m) return set_err(c, dbx::fail(DBX_ERR_MODEL, "unknown model id"));
+  if (row < 0 || col < row || col >= m->nspecies)
+    return set_err(c, dbx::fail(DBX_ERR_ARG, "need 0 <= row <= col < nspecies"));
+  c->arena.reset();  // the previous call ended synchronised
+  Error e = grow(c, &c->tmp_hist, sizeof(unsigned long long) * (size_t)nbins);
+  if (e.code) return set_err(c, e);
+  size_t delta = 0;
+  e = dbx::hist_plain(*m, row, col, (float)(1.0 / rstep), nbins,
+                      (unsigned long long *)c->tmp_hist.p, &c->hws, c->stream,
+                      &delta);
+  c->used += delta;
+  if (e.code) return set_err(c, e);
+  c->d2h += sizeof(unsigned long long);
+  // the counts below nbins are copied out before the range check reports
+  const Error ce = copy_rows(c, (const unsigned long long *)c->tmp_hist.p,
+                             nbins, nbins, 1, out);
+  if (ce.code) return set_err(c, ce);
+  return set_err(c, dbx::hist_range_check(c->hws, c->stream));
+}
+
 int dbx_histogram(dbx_ctx *c, int64_t id, double rstep, int64_t nbins,
                   int64_t *out) {
   if (!c || !out || !(rstep > 0)) return DBX_ERR_ARG;

@@ -25,11 +25,18 @@
 // On the first call on a device, that device current, the entry point looks
 // up the array's device address with cudaGetSymbolAddress (a host-side
 // name of a __device__ array is not a device address). That first call
-// should therefore come before any stream capture.
+// should therefore come before any stream capture. Every call waits for its
+// stream to finish the call's work before it returns (it reads back the
+// out-of-range count), so it blocks the calling host thread.
+//
+// A range paired with itself is recognised by equal starts, as the
+// reference's splitCalcDist does (cuDebye-v15.cu:241); equal starts with
+// different counts name no species block and are rejected.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/cudebye.h"
@@ -237,16 +244,30 @@ extern "C" int dbx_pair_histogram_noalloc(const float *x, const float *y,
   if (!x || !y || !z || !out || a_start < 0 || b_start < 0 || a_count < 0 ||
       b_count < 0 || !(rstep > 0) || nbins < 1 || nbins > (int64_t(1) << 22))
     return DBX_ERR_ARG;
-  // The reference's `dist` kernel serves a block paired with itself
-  // (cuDebye-v15.cu:243): pairs j <= i including i == j.
-  const bool diag = a_start == b_start && a_count == b_count;
+  // The reference's `dist` kernel serves a block paired with itself, chosen
+  // by equal starts (cuDebye-v15.cu:241-243): pairs j <= i including i == j.
+  const bool diag = a_start == b_start;
+  if (diag && a_count != b_count) return DBX_ERR_ARG;
+  // each count alone first, so that the sum below cannot overflow
+  if (a_count > kNoAllocMaxAtoms || b_count > kNoAllocMaxAtoms) return DBX_ERR_LIMIT;
   const int64_t natoms = diag ? a_count : a_count + b_count;
   if (natoms > kNoAllocMaxAtoms) return DBX_ERR_LIMIT;
+  // index ranges must fit the 64-bit arithmetic of pack_kernel
+  if (a_start > INT64_MAX - a_count || b_start > INT64_MAX - b_count)
+    return DBX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   int dev = 0, nsm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
-          cudaSuccess)
+  if (cudaGetDevice(&dev) != cudaSuccess) return DBX_ERR_CUDA;
+  // The scratch address below is the current device's; a stream of another
+  // device is refused (the legacy default stream, NULL, is the current
+  // device's).
+  if (s) {
+    int sdev = -1;
+    if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) return DBX_ERR_CUDA;
+    if (sdev != dev) return DBX_ERR_ARG;
+  }
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
+      cudaSuccess)
     return DBX_ERR_CUDA;
   unsigned char *base = nullptr;
   int rc = setup(dev, &base);

@@ -98,9 +98,15 @@ class SynthModel:
 
 def xyz2deb_rmax(xyz):
     """Rmax = 2*ceil(1.025*max|r|) after centring (Matlab/xyz2deb.m:198-204)."""
+    if not len(xyz):
+        return 0
     x = xyz.astype(np.float64)
     c = (x.max(axis=0) + x.min(axis=0)) / 2
-    r = np.sqrt(((x - c) ** 2).sum(axis=1)).max() if len(x) else 0.0
+    d = x - c
+    d *= d
+    # the square root of the largest squared distance: the same value as the
+    # largest square root (sqrt is correctly rounded and monotonic)
+    r = math.sqrt(float((d[:, 0] + d[:, 1] + d[:, 2]).max()))
     return 2 * math.ceil(r * 1.025)
 
 
@@ -206,8 +212,7 @@ def random_model(rng, nmin, nmax, grid, label, seed):
     elif kind == 1:
         basis, a = FCC, 4.05
     else:
-        basis = FCC + [tuple(v / 2 for v in t) for t in TET[:2]] + OCT[:2]
-        a = 3.95
+        basis, a = SPINEL_LIKE, 3.95
     dens = len(basis) / a ** 3
     radius = (3 * n / (4 * math.pi * dens)) ** (1 / 3) + 2 * a
     sites = _closest(_cube_sites(basis, a, radius), n, rng)
@@ -225,9 +230,86 @@ def batch256(seed=3, nmodels=256, nmin=2000, nmax=60000):
             for i in range(nmodels)]
 
 
+SPINEL_LIKE = FCC + [tuple(v / 2 for v in t) for t in TET[:2]] + OCT[:2]
+
+
+class RequestStream:
+    """Fresh serving requests at a small host cost, for arrival rates of
+    hundreds per second: per lattice (sc a=2.0, fcc a=4.05, spinel-like
+    a=3.95, as random_model) the sites of a sphere big enough for the
+    largest request are generated and ordered by distance from the centre
+    once. A request takes its N closest sites (N log-uniform), turns them by
+    a random rotation, adds its own Gaussian jitter (sigma U[0.03, 0.1]),
+    draws 1-4 species (each site's species uniform: a per-site random label
+    drawn once, offset at random per request), B U[0.2, 1.5], and its own
+    2theta grid of 2,000-20,000 points. No two requests share a geometry."""
+
+    def __init__(self, rng, nmin=1000, nmax=200000):
+        self.rng, self.nmin, self.nmax = rng, nmin, nmax
+        self.sites = []
+        for basis, a in ((SC, 2.0), (FCC, 4.05), (SPINEL_LIKE, 3.95)):
+            dens = len(basis) / a ** 3
+            radius = (3 * nmax / (4 * math.pi * dens)) ** (1 / 3) + 2 * a
+            self.sites.append(_closest(_cube_sites(basis, a, radius), nmax, rng))
+        # per site a uniform label in [0, 12): (label + offset) mod nsp is a
+        # uniform species for nsp = 1..4 (12 is their least common multiple)
+        self.labels = [rng.integers(0, 12, size=nmax).astype(np.int8)
+                       for _ in self.sites]
+
+    def next(self):
+        rng = self.rng
+        kind = int(rng.integers(3))
+        n = int(round(math.exp(rng.uniform(math.log(self.nmin),
+                                           math.log(self.nmax)))))
+        nsp = int(rng.integers(1, 5))
+        sigma = float(rng.uniform(0.03, 0.1))
+        npts = int(rng.integers(2000, 20001))
+        q, r = np.linalg.qr(rng.normal(size=(3, 3)))
+        rot = q * np.sign(np.diag(r))  # a uniformly random orthogonal matrix
+        # species of each site (uniform), atoms grouped by species
+        lab = (self.labels[kind][:n] + np.int8(rng.integers(12))) % np.int8(nsp)
+        order = np.argsort(lab, kind="stable")
+        counts = np.bincount(lab, minlength=nsp).tolist()
+        xyz = self.sites[kind][order] @ rot.T
+        xyz += rng.normal(0.0, sigma, size=xyz.shape)
+        xyz = xyz.astype(np.float32)
+        keep = [i for i, c in enumerate(counts) if c > 0]
+        names = [POOL[i] for i in keep]
+        params = [species(nm, 1.0, float(rng.uniform(0.2, 1.5))) for nm in names]
+        grid = (1.5406, 10.0, 130.0, 120.0 / (npts - 1))
+        return SynthModel(xyz, [counts[i] for i in keep], names, params, 1e-3,
+                          xyz2deb_rmax(xyz), *grid, None, "request")
+
+
 def serving_request(rng, nmin=1000, nmax=200000):
     """One serving request: a model with its own 2theta grid of 2k-20k
     points (2theta 10-130 at 1.5406 A, step chosen for the point count)."""
     npts = int(rng.integers(2000, 20001))
     grid = (1.5406, 10.0, 130.0, 120.0 / (npts - 1))
     return random_model(rng, nmin, nmax, grid, "request", None)
+
+
+def request_worker(seed, out, stop):
+    """Process target (start it with the "spawn" method): RequestStream
+    requests, put on the queue `out` as plain tuples (model_from_item turns
+    them back into models) until the event `stop` is set."""
+    import queue as queue_mod
+    rs = RequestStream(np.random.default_rng(seed))
+    while not stop.is_set():
+        m = rs.next()
+        item = (m.xyz, m.counts, m.names, [s.beq for s in m.species], m.rmax,
+                m.tt_step)
+        while not stop.is_set():
+            try:
+                out.put(item, timeout=0.1)
+                break
+            except queue_mod.Full:
+                continue
+
+
+def model_from_item(item):
+    """The SynthModel of a request_worker tuple."""
+    xyz, counts, names, beqs, rmax, tt_step = item
+    params = [species(nm, 1.0, b) for nm, b in zip(names, beqs)]
+    return SynthModel(xyz, counts, names, params, 1e-3, rmax, 1.5406, 10.0,
+                      130.0, tt_step, None, "request")

@@ -108,6 +108,14 @@ int dbx_model_free(dbx_ctx *ctx, int64_t model_id);
 int dbx_pair_histogram(dbx_ctx *ctx, int64_t model_id, int row, int col,
                        double rstep, int64_t nbins, int64_t *out_counts);
 
+/* The same histogram computed by the plain unbatched FP32 GPU form: one
+ * thread per atom pair with one global 64-bit atomicAdd, in the
+ * reference's launch shape (dist / dist2, cuDebye-v15.cu:88-146). The
+ * comparison baseline only; bit-exact with dbx_pair_histogram. On
+ * DBX_ERR_RANGE out_counts still holds the pairs binned below nbins. */
+int dbx_pair_histogram_plain(dbx_ctx *ctx, int64_t model_id, int row, int col,
+                             double rstep, int64_t nbins, int64_t *out_counts);
+
 /* All P(P+1)/2 pair histograms in one device pass, out_counts
  * [npairs][nbins] in pair order (the pair loop cuDebye-v15.cu:941-967). */
 int dbx_histogram(dbx_ctx *ctx, int64_t model_id, double rstep, int64_t nbins,
@@ -127,15 +135,19 @@ int dbx_histogram(dbx_ctx *ctx, int64_t model_id, double rstep, int64_t nbins,
  *
  * Inputs are the reference's device arrays and index ranges: x, y, z
  * (float, device) and the atom ranges [a_start, a_start+a_count) and
- * [b_start, b_start+b_count); a range paired with itself (a_start ==
- * b_start and equal counts) counts pairs j <= i including i == j, like the
- * reference's `dist` kernel. out (int64, device, nbins entries) receives
- * the histogram, bit-exact with dbx_pair_histogram. stream is a
- * cudaStream_t (NULL: the legacy default stream); the call returns after
- * the stream has finished it.
+ * [b_start, b_start+b_count). Equal starts mean a range paired with itself
+ * (the reference's rule, cuDebye-v15.cu:241): it counts pairs j <= i
+ * including i == j, like the reference's `dist` kernel, and needs equal
+ * counts (else DBX_ERR_ARG). out (int64, device, nbins entries) receives
+ * the histogram, bit-exact with dbx_pair_histogram; with DBX_ERR_RANGE it
+ * still holds the pairs that binned below nbins. stream is a cudaStream_t
+ * of the current device (NULL: the legacy default stream; a stream of
+ * another device gives DBX_ERR_ARG). Every call waits for the stream to
+ * finish its work before returning, so it blocks the calling thread.
  *
  * Limits: at most DBX_NOALLOC_MAX_ATOMS atoms (a_count + b_count, or a_count
- * for a range with itself), else DBX_ERR_LIMIT; nbins <= 4194304.
+ * for a range with itself; each count is checked alone first), else
+ * DBX_ERR_LIMIT; nbins <= 4194304.
  * The first call on a device looks up the scratch array's device address
  * (with that device current), so make it before any stream capture. All
  * calls share the array and leave their data in it; each call clears what

@@ -61,6 +61,30 @@ def test_host_entry_points_without_gpu(built_lib):
         assert rc == -2 and not ctx
 
 
+def test_noalloc_argument_checks_without_gpu(built_lib):
+    """dbx_pair_histogram_noalloc refuses bad requests before any CUDA call:
+    counts whose sum would overflow int64, a single count above the limit,
+    equal starts with different counts, negative sizes. Run only where there
+    is no GPU, so that the placeholder pointers can never reach a device."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("placeholder pointers: CPU-only check")
+    except ImportError:
+        pass
+    lib = cd.load_library(built_lib)
+    f = lib.dbx_pair_histogram_noalloc
+    p = ctypes.c_void_p(16)
+    big = (1 << 62) + 1  # a_count + b_count overflows int64
+    assert f(p, p, p, 0, big, 1, big, 1e-3, 10, p, None) == -11
+    assert f(p, p, p, 0, 1834993, 2000000, 1, 1e-3, 10, p, None) == -11
+    assert f(p, p, p, 0, 1, 2000000, 1834992, 1e-3, 10, p, None) == -11
+    assert f(p, p, p, 5, 10, 5, 11, 1e-3, 10, p, None) == -1
+    assert f(p, p, p, 0, -1, 10, 1, 1e-3, 10, p, None) == -1
+    assert f(p, p, p, 0, 1, 10, 1, 0.0, 10, p, None) == -1
+    assert f(p, p, p, 0, 1, 10, 1, 1e-3, 0, p, None) == -1
+
+
 def test_tile_order_is_a_hilbert_curve(built_lib):
     """The curve that orders atoms into tiles visits every cell of the
     2^bits cube once, each step to a face neighbour (so runs of it, the

@@ -8,9 +8,10 @@ __device__ array. This test drives it through the C ABI with device
 buffers the test itself owns (allocated here by torch, as such a caller's
 host framework would) and checks, on two calls in a row that reuse the
 shared scratch, that its histograms equal dbx_pair_histogram's bin for bin
-(the histogram is integer: the tolerance is exact equality). It also
-checks the size limit. Collected last so that a failure here cannot stop
-the other tests of a run that stops at the first failure.
+(the histogram is integer: the tolerance is exact equality), then the CPU
+oracle's on ragged and edge cases, and the size limit with device buffers
+as large as the request claims. Collected last so that a failure here
+cannot stop the other tests of a run that stops at the first failure.
 """
 import ctypes
 
@@ -25,11 +26,15 @@ pytestmark = pytest.mark.gpu
 DBX_NOALLOC_MAX_ATOMS = 1834992  # include/cudebye.h
 
 
-def noalloc(engine, torch, xyz, a0, na, b0, nb, rstep, nbins):
+def device_xyz(torch, xyz):
     dev = torch.device("cuda", 0)
-    x = torch.tensor(np.ascontiguousarray(xyz[:, 0]), device=dev)
-    y = torch.tensor(np.ascontiguousarray(xyz[:, 1]), device=dev)
-    z = torch.tensor(np.ascontiguousarray(xyz[:, 2]), device=dev)
+    return [torch.tensor(np.ascontiguousarray(xyz[:, c]), device=dev)
+            for c in range(3)]
+
+
+def call(engine, torch, xyzd, a0, na, b0, nb, rstep, nbins):
+    dev = torch.device("cuda", 0)
+    x, y, z = xyzd
     out = torch.full((nbins,), -7, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream(dev)
     rc = engine.lib.dbx_pair_histogram_noalloc(
@@ -37,6 +42,11 @@ def noalloc(engine, torch, xyz, a0, na, b0, nb, rstep, nbins):
         ctypes.c_void_p(z.data_ptr()), a0, na, b0, nb, rstep, nbins,
         ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
     return rc, out.cpu().numpy()
+
+
+def noalloc(engine, torch, xyz, a0, na, b0, nb, rstep, nbins):
+    return call(engine, torch, device_xyz(torch, xyz), a0, na, b0, nb, rstep,
+                nbins)
 
 
 def reference_entry(engine, xyz, counts, row, col, rstep, nbins):
@@ -47,9 +57,12 @@ def reference_entry(engine, xyz, counts, row, col, rstep, nbins):
         m.free()
 
 
+def starts(c):
+    return np.concatenate([[0], np.cumsum(c)[:-1]]).astype(int)
+
+
 def test_noalloc_equals_pair_histogram_twice(engine):
     torch = pytest.importorskip("torch")
-    starts = lambda c: np.concatenate([[0], np.cumsum(c)[:-1]]).astype(int)
     # call 1: an off-diagonal species block, one shared-memory window
     m1 = lattice.spinel(radius=14.0, target=2500, seed=31)
     s1 = starts(m1.counts)
@@ -71,10 +84,50 @@ def test_noalloc_equals_pair_histogram_twice(engine):
     assert int(got.sum()) == m2.counts[1] * (m2.counts[1] + 1) // 2
 
 
+def test_noalloc_edge_cases_match_oracle(engine, orc):
+    """Ragged blocks against the CPU oracle: an odd bin count whose last
+    window ends in a half-used counter word, an empty range, and a range
+    error spread over several windows (the in-range bins still counted)."""
+    torch = pytest.importorskip("torch")
+    m = lattice.spinel(radius=13.0, target=2100, seed=33, rstep=1e-4)
+    s = starts(m.counts)
+    xyzd = device_xyz(torch, m.xyz)
+    # odd nbins over three windows (the last one ends on a low half)
+    nb_odd = 2 * 114688 + 1001
+    assert nb_odd % 2 == 1
+    rc, got = call(engine, torch, xyzd, s[0], m.counts[0], s[2], m.counts[2],
+                   1e-4, nb_odd)
+    want, bad = orc.block_histogram(m.xyz, s[0], m.counts[0], s[2],
+                                    m.counts[2], False, 1e-4, nb_odd)
+    assert bad == 0 and rc == 0, cd.ERRORS.get(rc, rc)
+    np.testing.assert_array_equal(got, want)
+    # an empty range: all zeros, no error
+    rc, got = call(engine, torch, xyzd, s[1], 0, s[2], m.counts[2], 1e-4, 999)
+    assert rc == 0 and not got.any()
+    # a range error over several windows: bins end below the largest
+    # distance; the pairs below nbins are still counted, bin for bin
+    nb_short = 2 * 114688 + 500
+    rc, got = call(engine, torch, xyzd, s[0], m.counts[0], s[0], m.counts[0],
+                   1e-4, nb_short)
+    want, bad = orc.block_histogram(m.xyz, s[0], m.counts[0], s[0],
+                                    m.counts[0], True, 1e-4, nb_short)
+    assert bad > 0
+    assert cd.ERRORS.get(rc) == "DBX_ERR_RANGE"
+    np.testing.assert_array_equal(got, want)
+
+
 def test_noalloc_rejects_oversized_request(engine):
     torch = pytest.importorskip("torch")
-    xyz = np.zeros((4, 3), np.float32)
+    # device coordinates as long as the request claims, so that no access
+    # could leave them even if the size check failed
+    n = DBX_NOALLOC_MAX_ATOMS + 1
+    xyzd = device_xyz(torch, np.zeros((n, 3), np.float32))
     # more atoms than the fixed scratch holds: refused before any GPU work
-    rc, _ = noalloc(engine, torch, xyz, 0, DBX_NOALLOC_MAX_ATOMS, 0,
-                    DBX_NOALLOC_MAX_ATOMS + 1, 1e-3, 100)
+    rc, _ = call(engine, torch, xyzd, 0, DBX_NOALLOC_MAX_ATOMS, DBX_NOALLOC_MAX_ATOMS,
+                 1, 1e-3, 100)
     assert cd.ERRORS.get(rc) == "DBX_ERR_LIMIT"
+    rc, _ = call(engine, torch, xyzd, 0, n, 0, n, 1e-3, 100)
+    assert cd.ERRORS.get(rc) == "DBX_ERR_LIMIT"
+    # equal starts with different counts name no species block
+    rc, _ = call(engine, torch, xyzd, 0, 10, 0, 11, 1e-3, 100)
+    assert cd.ERRORS.get(rc) == "DBX_ERR_ARG"
