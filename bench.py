@@ -324,9 +324,9 @@ def batch_bench(eng, steps=5, seed=3, nmodels=256, plain_models=None):
 def precision_bench(eng, reps=3):
     """The precision form: the spinel model's histograms (resident) summed
     on the 20,000-point q grid (2theta 5-150 deg at 0.7107 A) by the exact
-    tensor-core split, the three-product BF16x3 form, the plain FP32
-    direct sum and the FP64 direct sum (the reference's arithmetic, the
-    error reference). Per form: device time of the Debye sum (CUDA events,
+    tensor-core split, the three-product BF16x3 and TF32-split forms, the
+    plain FP32 direct sum and the FP64 direct sum (the reference's
+    arithmetic, the error reference). Per form: device time of the Debye sum (CUDA events,
     median of `reps`) and max relative error over all q."""
     from cudebye_gb300 import lattice
     m = lattice.precision()
@@ -336,7 +336,7 @@ def precision_bench(eng, reps=3):
     try:
         eng.histogram(mod, m.rstep, m.nbins)
         outs = {}
-        for mode in ("fp64", "tc", "tc3", "fp32"):
+        for mode in ("fp64", "tc", "tc3", "tf32", "fp32"):
             ts, ws = [], []
             for _ in range(reps + 1):
                 t0 = time.perf_counter()
@@ -347,7 +347,7 @@ def precision_bench(eng, reps=3):
             res[mode] = {"debye_kernel_ms": float(np.median(ts[1:])),
                          "call_ms": float(np.median(ws[1:])) * 1e3}
         ref = outs["fp64"]
-        for mode in ("tc", "tc3", "fp32"):
+        for mode in ("tc", "tc3", "tf32", "fp32"):
             rel = np.abs(outs[mode] - ref) / np.abs(ref)
             res[mode]["max_rel_err"] = float(np.max(rel))
             res[mode]["median_rel_err"] = float(np.median(rel))
@@ -358,11 +358,13 @@ def precision_bench(eng, reps=3):
             "bins": m.nbins, "pair_types": len(m.counts) * (len(m.counts) + 1) // 2,
             "error_reference": "fp64 direct sum (device)",
             "timing": "debye_kernel_ms: CUDA events around the contraction "
-                      "kernel (tc, tc3) or the direct-sum kernel; call_ms: "
+                      "kernel (tc, tc3, tf32) or the direct-sum kernel; call_ms: "
                       "host wall clock of dbx_intensity on resident "
                       "histograms (prefactors, weights, reduction, D2H)",
             "forms": {"tc": "exact 4-digit bf16 split (10 products)",
                       "tc3": "BF16x3: 2 digits, 3 products",
+                      "tf32": "TF32-split: tf32 hi/lo parts, 3 products, FP32 "
+                              "accumulation per 256-bin chunk, FP64 chunk sums",
                       "fp32": "FP32 direct sum", "fp64": "FP64 direct sum"},
             "results": res}
 
@@ -943,6 +945,10 @@ def run_engine(args):
                 "rate", "submitted", "patterns_per_s", "p50_ms", "p99_ms")}
             ns["serving"]["saturation_req_per_s"] = \
                 line["serving"]["saturation_req_per_s"]
+    if "precision" in line:
+        r = line["precision"]["results"]
+        ns["precision_20000q_max_rel_err"] = {
+            k: sig(r[k]["max_rel_err"], 2) for k in ("tc", "tf32", "tc3", "fp32")}
     if "plain_small" in line:
         ns["plain_small"] = {"value": sig(line["plain_small"]["value"]),
                              "e2e": sig(line["plain_small"]["e2e"]["value"])}

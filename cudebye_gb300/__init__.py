@@ -40,7 +40,7 @@ ERRORS = {
     -7: "DBX_ERR_RANGE", -8: "DBX_ERR_MODEL", -9: "DBX_ERR_TIMEOUT",
     -10: "DBX_ERR_IO", -11: "DBX_ERR_LIMIT",
 }
-MODES = {"tc": 0, "fp64": 1, "fp32": 2, "plain": 3, "tc3": 4}
+MODES = {"tc": 0, "fp64": 1, "fp32": 2, "plain": 3, "tc3": 4, "tf32": 5}
 
 # Every symbol include/cudebye.h declares (checked by the CPU tests).
 EXPORTS = (

@@ -38,6 +38,7 @@ struct BatchState {
   cudaGraphExec_t exec = nullptr;
   std::vector<const void *> graph_ptrs;  // buffers the graph was built on
   int tuned_tasks = 0;
+  uint64_t tc_gen = 0;  // the contraction state's preparation of this batch
   bool valid = false;
 };
 
@@ -210,8 +211,8 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
                 double *out_I) {
   if (nq < 1) return dbx::fail(DBX_ERR_ARG, "nq must be >= 1");
   c->arena.reset();  // the previous call ended synchronised
-  if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_TC3 && mode != DBX_DEBYE_FP64 &&
-      mode != DBX_DEBYE_FP32)
+  if (mode != DBX_DEBYE_TC && mode != DBX_DEBYE_TC3 && mode != DBX_DEBYE_TF32 &&
+      mode != DBX_DEBYE_FP64 && mode != DBX_DEBYE_FP32)
     return dbx::fail(DBX_ERR_ARG, "unknown Debye mode");
   bool launched = false;
   DBX_TRY(ensure_hist(c, m, rstep, nbins, &launched));
@@ -227,7 +228,7 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   DBX_TRY(dbx::debye_prefactor(sp, m->nspecies, (const double *)c->K.p, nq,
                                (double *)c->ff.p, c->stream, &c->arena));
   c->tm.stop(DBX_T_PREFACTOR, c->stream);
-  if (mode == DBX_DEBYE_TC || mode == DBX_DEBYE_TC3) {
+  if (mode == DBX_DEBYE_TC || mode == DBX_DEBYE_TC3 || mode == DBX_DEBYE_TF32) {
     std::vector<dbx::TcCol> cols(np);
     for (int p = 0; p < np; ++p) {
       cols[p].hist = m->d_hist + (size_t)p * m->hist_pitch;
@@ -236,11 +237,11 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
     }
     size_t delta = 0;
     const int64_t h0 = c->tc.h2d, d0 = c->tc.d2h;
-    c->tc.classes = mode == DBX_DEBYE_TC3 ? 2 : 4;
+    c->tc.form = mode == DBX_DEBYE_TC3 ? 1 : mode == DBX_DEBYE_TF32 ? 2 : 0;
     Error e = dbx::debye_tc(&c->tc, cols, {0, np}, rstep, K,
                             (const double *)c->K.p, nq, (double *)c->I.p,
                             c->stream, &delta, &c->tm);
-    c->tc.classes = 4;
+    c->tc.form = 0;
     c->used += delta;
     c->h2d += c->tc.h2d - h0;
     c->d2h += c->tc.d2h - d0;
@@ -361,7 +362,10 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
   for (int i = 0; i < nm; ++i) DBX_TRY(alloc_hist(c, ms[i], nbins[i]));
   std::vector<const void *> hist_ptrs(nm);
   for (int i = 0; i < nm; ++i) hist_ptrs[i] = ms[i]->d_hist;
-  const bool same = b.valid && b.rstep == rstep && b.K.size() == (size_t)nq &&
+  // (the contraction state is shared with single-pattern calls: a batch
+  // is replayed only if no other call prepared a contraction since)
+  const bool same = b.valid && b.tc_gen == c->tc.prep_gen && b.rstep == rstep &&
+                    b.K.size() == (size_t)nq &&
                     b.ids == std::vector<int64_t>(ids, ids + nm) &&
                     b.nbins == std::vector<int64_t>(nbins, nbins + nm) &&
                     b.hist_ptrs == hist_ptrs &&
@@ -422,6 +426,7 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
     c->used += delta;
     delta = 0;
     if (e.code) return e;
+    b.tc_gen = c->tc.prep_gen;
     e = dbx::hist_scratch(b.hp.plan, &c->hws, &delta);
     c->used += delta;
     delta = 0;

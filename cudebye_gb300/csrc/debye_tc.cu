@@ -35,6 +35,16 @@
 // N=64, K=16) into one of two TMEM accumulator sets (4 classes x 64 f32
 // columns each) and commits, four epilogue warps drain the other set.
 // Every wait is bounded and reports a timeout through an error word.
+//
+// Two comparison forms share the kernel: BF16x3 (two 8-bit digits per
+// operand, products (0,0), (0,1), (1,0)) and TF32x3: each operand's
+// fixed-point value x is split into tf32 parts hi = tf32(x), lo =
+// tf32(x - hi) (22 significant bits together), stored as fp32 in the same
+// slab bytes (two 32-bit parts take the room of four 16-bit digits), and
+// multiplied with tcgen05.mma kind::tf32 (K = 8) as hi*hi into one
+// accumulator and hi*lo + lo*hi into another, with FP32 accumulation over
+// the chunk's 256 bins; the lo*lo term and the FP32 rounding of the sums are
+// its error. Neither form is exact; the exact split is the default.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -60,6 +70,17 @@ constexpr int kASlabBytes = kND * kABlock * 2;  // 64 KB
 constexpr int kBSlabBytes = kND * kBBlock * 2;  // 32 KB
 constexpr int kTmemCols = 256;      // 4 classes x 64 columns
 constexpr double kSelfR = 0.0005;   // cuDebye-v15.cu:508
+// TF32 operands: two fp32 parts per value in the bytes of four bf16 digits.
+constexpr int kNP32 = 2;
+static_assert(kNP32 * kABlock * 4 == kASlabBytes, "tf32 A parts fill the slab");
+static_assert(kNP32 * kBBlock * 4 == kBSlabBytes, "tf32 W parts fill the slab");
+
+// Operand forms of the contraction (TcState::form).
+constexpr int kFormExact = 0;   // 4 bf16 digits, 10 products: exact
+constexpr int kFormBf16x3 = 1;  // 2 bf16 digits, 3 products
+constexpr int kFormTf32x3 = 2;  // 2 tf32 parts, 3 products
+__host__ __device__ constexpr int form_classes(int f) { return f == kFormExact ? 4 : 2; }
+__host__ __device__ constexpr bool form_tf32(int f) { return f == kFormTf32x3; }
 
 // Element offset of (row, k) inside a [rows x 64] block stored as 8x8
 // core matrices (8 rows x 16 bytes each, contiguous), row groups outermost:
@@ -67,6 +88,29 @@ constexpr double kSelfR = 0.0005;   // cuDebye-v15.cu:508
 // stride (row-group) byte offset 1024.
 __host__ __device__ inline int tiled_off(int row, int k) {
   return ((((row >> 3) << 3) + (k >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
+}
+
+// The same for 32-bit elements (8 rows x 4 elements per core matrix): core
+// (g, kc) at (g*16 + kc)*32 elements. Leading byte offset 128, stride
+// byte offset 2048.
+__host__ __device__ inline int tiled_off32(int row, int k) {
+  return ((((row >> 3) << 4) + (k >> 2)) << 5) + ((row & 7) << 2) + (k & 3);
+}
+
+// Nearest tf32 (10 explicit mantissa bits; ties away from zero) of a
+// finite float: the tensor core reads only those bits of an fp32 operand.
+__device__ inline float tf32_rn(float f) {
+  return __uint_as_float((__float_as_uint(f) + 0x1000u) & 0xFFFFE000u);
+}
+
+// tf32 parts of the fixed-point value v 2^-24 (|v| < 2^31): hi + lo equals
+// it to about 2^-22 relative. The scale 2^-24 makes the products' sums
+// carry the weight of the exact form's top digit pair (2^48 over the
+// product of two 31-bit fixed-point values), so the epilogue is shared.
+__device__ inline void split_tf32(long long v, float &hi, float &lo) {
+  const double x = (double)v * 0x1p-24;  // exact
+  hi = tf32_rn((float)x);
+  lo = tf32_rn((float)(x - (double)hi));
 }
 
 // Balanced base-256 digits of v, |v| <= 2^31 - 1, most significant first:
@@ -100,6 +144,9 @@ constexpr int kRun = 16;
 // Basis digits: rows [0,Qp) cos(K_q j dr), rows [Qp,2Qp) sin(K_q j dr).
 // Layout: [row tile][slab][digit][tiled 128 x 64]. One thread per row and
 // run of kRun columns; eight columns of a digit are one 16-byte store.
+// TF32: [row tile][slab][part][tiled32 128 x 64] fp32, four columns of a
+// part per 16-byte store.
+template <bool TF32>
 __global__ void basis_kernel(const double *__restrict__ K, int nq, int Qp,
                              double rstep, __nv_bfloat16 *__restrict__ A) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,6 +161,28 @@ __global__ void basis_kernel(const double *__restrict__ K, int nq, int Qp,
     sincos(K[q] * rstep, &ss, &cs);
   }
   const int mt = m / kTM, row = m % kTM;
+  if (TF32) {
+    float *A32 = reinterpret_cast<float *>(A);
+#pragma unroll
+    for (int g = 0; g < kRun; g += 4) {
+      alignas(16) float part[kNP32][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        split_tf32(fixed31(sinrow ? s : c), part[0][i], part[1][i]);
+        const double s2 = fma(s, cs, c * ss), c2 = fma(c, cs, -(s * ss));
+        s = s2;
+        c = c2;
+      }
+      const int j = j0 + g, ks = j / kKS, k = j % kKS;
+      const size_t base =
+          (size_t)(mt * kNSlab + ks) * kNP32 * kABlock + tiled_off32(row, k);
+#pragma unroll
+      for (int t = 0; t < kNP32; ++t)
+        *reinterpret_cast<float4 *>(A32 + base + (size_t)t * kABlock) =
+            *reinterpret_cast<const float4 *>(part[t]);
+    }
+    return;
+  }
 #pragma unroll
   for (int g = 0; g < kRun; g += 8) {
     alignas(16) __nv_bfloat16 dig[kND][8];
@@ -136,10 +205,12 @@ __global__ void basis_kernel(const double *__restrict__ K, int nq, int Qp,
   }
 }
 
-// Twiddles per (chunk, q): alpha = K_q * ch*L*dr; (sin hi, sin lo, cos hi,
-// cos lo) as double-floats. One thread per q and run of kRun chunks.
+// Twiddles per (chunk, q): alpha = K_q * ch*L*dr, as double-floats in two
+// planes: tw[ch*Qp + q] = (sin hi, sin lo), tw[(nch + ch)*Qp + q] = (cos hi,
+// cos lo) (a cosine row of the contraction reads only the sine plane, a
+// sine row only the cosine plane). One thread per q and run of kRun chunks.
 __global__ void twiddle_kernel(const double *__restrict__ K, int nq, int Qp,
-                               int nch, double rstep, float4 *__restrict__ tw) {
+                               int nch, double rstep, float2 *__restrict__ tw) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)(nch / kRun) * Qp) return;
   const int q = (int)(idx % Qp);
@@ -152,8 +223,8 @@ __global__ void twiddle_kernel(const double *__restrict__ K, int nq, int Qp,
 #pragma unroll 4
   for (int i = 0; i < kRun; ++i) {
     const float sh = (float)s, ch_ = (float)c;
-    tw[(size_t)(ch0 + i) * Qp + q] =
-        make_float4(sh, (float)(s - (double)sh), ch_, (float)(c - (double)ch_));
+    tw[(size_t)(ch0 + i) * Qp + q] = make_float2(sh, (float)(s - (double)sh));
+    tw[(size_t)(nch + ch0 + i) * Qp + q] = make_float2(ch_, (float)(c - (double)ch_));
     const double s2 = fma(s, cs, c * ss), c2 = fma(c, cs, -(s * ss));
     s = s2;
     c = c2;
@@ -168,7 +239,9 @@ __global__ void twiddle_kernel(const double *__restrict__ K, int nq, int Qp,
 // round(n_k 2^(31-e) / k), with e the chunk's scale exponent (every
 // u_k < 2^e). No FP64 arithmetic (slow on this part) is needed.
 // Layout of W: [col tile][slab][digit][tiled 64 x 64]; E: per column,
-// the chunk's scale exponent.
+// the chunk's scale exponent. TF32: [col tile][slab][part][tiled32 64 x 64]
+// fp32 parts of the same fixed-point values.
+template <bool TF32>
 __global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
                                const TcCol *__restrict__ cols, long long kself,
                                __nv_bfloat16 *__restrict__ W,
@@ -210,8 +283,7 @@ __global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
     if (__any_sync(0xffffffffu, over)) ++e;
   }
   const int j0 = lane * 8, ks = j0 / kKS, k0 = j0 % kKS;
-  const size_t base = (size_t)(nt * kNSlab + ks) * kND * kBBlock + tiled_off(n, k0);
-  alignas(16) __nv_bfloat16 dig[kND][8];
+  long long fx[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     long long f = 0;
@@ -223,15 +295,37 @@ __global__ void weights_kernel(const TcTile *__restrict__ tiles, int ntiles,
       f = (long long)((num + den / 2) / den);
       f = f > 2147483647LL ? 2147483647LL : f;
     }
-    float d[4];
-    split4(f, d);
-#pragma unroll
-    for (int s = 0; s < kND; ++s) dig[s][i] = __float2bfloat16_rn(d[s]);
+    fx[i] = f;
   }
+  if (TF32) {
+    float *W32 = reinterpret_cast<float *>(W);
+    const size_t base = (size_t)(nt * kNSlab + ks) * kNP32 * kBBlock;
 #pragma unroll
-  for (int s = 0; s < kND; ++s)
-    *reinterpret_cast<uint4 *>(W + base + (size_t)s * kBBlock) =
-        *reinterpret_cast<const uint4 *>(dig[s]);
+    for (int h = 0; h < 2; ++h) {  // columns k0 + 4h .. k0 + 4h + 3
+      alignas(16) float part[kNP32][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) split_tf32(fx[4 * h + i], part[0][i], part[1][i]);
+#pragma unroll
+      for (int t = 0; t < kNP32; ++t)
+        *reinterpret_cast<float4 *>(W32 + base + (size_t)t * kBBlock +
+                                    tiled_off32(n, k0 + 4 * h)) =
+            *reinterpret_cast<const float4 *>(part[t]);
+    }
+  } else {
+    const size_t base = (size_t)(nt * kNSlab + ks) * kND * kBBlock + tiled_off(n, k0);
+    alignas(16) __nv_bfloat16 dig[kND][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float d[4];
+      split4(fx[i], d);
+#pragma unroll
+      for (int s = 0; s < kND; ++s) dig[s][i] = __float2bfloat16_rn(d[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < kND; ++s)
+      *reinterpret_cast<uint4 *>(W + base + (size_t)s * kBBlock) =
+          *reinterpret_cast<const uint4 *>(dig[s]);
+  }
   if (lane == 0) {
     E[nt * kTN + n] = e;
     if (any) atomicOr(&nonself[t.col], 1);
@@ -268,10 +362,11 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo,
   return d;                // base offset 0, no swizzle
 }
 
-// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major.
-__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor of kind::f16 (A/B bf16: format 1) or kind::tf32
+// (A/B tf32: format 2): D f32, both operands K-major, M x N.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N, bool tf32 = false) {
+  return (1u << 4) | ((tf32 ? 2u : 1u) << 7) | ((tf32 ? 2u : 1u) << 10) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t ad,
@@ -280,6 +375,15 @@ __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t ad,
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t ad,
+                                         uint64_t bd, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
       "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
 
@@ -324,19 +428,24 @@ constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
 // Epilogue of one tile for TMEM lane `row` (0..127) of accumulator set at
 // column offset acc_col: D = acc0 + acc1 2^-8 + acc2 2^-16 + acc3 2^-24,
 // scaled, rotated by the chunk twiddle and summed over the tile's 64 chunks.
-template <int NCLS>
+template <int FORM>
 __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
                                                 int mt, int nt,
                                                 const TcTile *__restrict__ tiles,
                                                 const int *__restrict__ Ecol,
-                                                const float4 *__restrict__ tw,
-                                                int Qp) {
+                                                const float2 *__restrict__ tw,
+                                                int Qp, int nchc) {
   const TcTile tile = tiles[nt];
   const int m = mt * kTM + row;
   const bool sinrow = m >= Qp;
   const int q = sinrow ? m - Qp : m;
-  const float4 *twq = tw + q;
+  // cosine rows are rotated by sin(q k0 dr), sine rows by cos(q k0 dr)
+  const float2 *twq = tw + (sinrow ? (size_t)nchc * Qp : 0) + q;
   const int *E = Ecol + nt * kTN;
+  constexpr int NCLS = form_classes(FORM);
+  // weight of accumulator 1 against accumulator 0: one base-256 digit, or
+  // none for the tf32 parts (hi*lo + lo*hi carry hi*hi's scale)
+  constexpr float kC1 = form_tf32(FORM) ? 1.0f : 0x1p-8f;
   float sh = 0.f, sl = 0.f;
 #pragma unroll 1
   for (int cg = 0; cg < kTN / 16; ++cg) {
@@ -358,15 +467,14 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
       const int n = cg * 16 + i;
       // exact two-sum of the top two classes, the rest rounded once
       const float c0 = __uint_as_float(a0[i]);
-      const float c1 = __uint_as_float(a1[i]) * 0x1p-8f;
+      const float c1 = __uint_as_float(a1[i]) * kC1;
       const float hi = c0 + c1;
       const float hb = hi - c0;
       const float lo = ((c0 - (hi - hb)) + (c1 - hb)) +
                        fmaf(__uint_as_float(a2[i]), 0x1p-16f,
                             __uint_as_float(a3[i]) * 0x1p-24f);
-      const float4 t = twq[(size_t)(tile.ch0 + n) * Qp];
-      const float th = sinrow ? t.z : t.x;
-      const float tl = sinrow ? t.w : t.y;
+      const float2 t = __ldg(&twq[(size_t)(tile.ch0 + n) * Qp]);
+      const float th = t.x, tl = t.y;
       // (th + tl) * (hi + lo) as a double-float, scaled by 2^(E-14)
       float p = th * hi;
       float pe = fmaf(th, hi, -p);
@@ -385,17 +493,19 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
   return (double)sh + (double)sl;
 }
 
-// NCLS = 4: the exact form (digit pairs with s + t <= 3). NCLS = 2: only the
-// pairs (0,0), (0,1), (1,0) — two 8-bit digits per operand and three
-// products, the BF16x3 scheme, kept for precision comparisons.
-template <int NCLS>
+// FORM kFormExact: the exact form (digit pairs with s + t <= 3, four
+// accumulators). kFormBf16x3: only the pairs (0,0), (0,1), (1,0) — two 8-bit
+// digits per operand and three products. kFormTf32x3: the same three
+// products of tf32 parts (kind::tf32, K = 8). The last two are kept for
+// precision comparisons.
+template <int FORM>
 __global__ void __launch_bounds__(kPThreads, 1)
     gemm_persistent_kernel(const __nv_bfloat16 *__restrict__ A,
                            const __nv_bfloat16 *__restrict__ W,
                            const TcTile *__restrict__ tiles,
                            const int *__restrict__ Ecol,
-                           const float4 *__restrict__ tw, int Qp, int nrt,
-                           int ntiles, double *__restrict__ P,
+                           const float2 *__restrict__ tw, int Qp, int nchc,
+                           int nrt, int ntiles, double *__restrict__ P,
                            int *__restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
@@ -467,7 +577,15 @@ __global__ void __launch_bounds__(kPThreads, 1)
       mbar_wait(bar(FULL + k % kPStages), (k / kPStages) & 1);
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    constexpr uint32_t idesc = make_idesc(kTM, kTN);
+    constexpr int NCLS = form_classes(FORM);
+    constexpr bool TF32 = form_tf32(FORM);
+    constexpr uint32_t idesc = make_idesc(kTM, kTN, TF32);
+    // bytes of one digit (part) block of A and W, and the MMA K step: 16
+    // bf16 or 8 tf32 elements, two core matrices (256 bytes) either way
+    constexpr int kAPart = TF32 ? kABlock * 4 : kABlock * 2;
+    constexpr int kBPart = TF32 ? kBBlock * 4 : kBBlock * 2;
+    constexpr int kSteps = TF32 ? kKS / 8 : kKS / 16;
+    constexpr uint32_t kSbo = TF32 ? 2048 : 1024;
     int it = 0, tc = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++tc) {
@@ -491,18 +609,21 @@ __global__ void __launch_bounds__(kPThreads, 1)
         // the field: shared addresses are below 256 KB), so each MMA needs
         // one add per operand instead of a descriptor build (the single
         // issuing thread limited the MMA rate)
-        const uint64_t adb = make_desc(sA, 128, 1024), bdb = make_desc(sB, 128, 1024);
+        const uint64_t adb = make_desc(sA, 128, kSbo), bdb = make_desc(sB, 128, kSbo);
 #pragma unroll
         for (int w = 0; w < NCLS; ++w) {
 #pragma unroll
           for (int s = 0; s <= w; ++s) {
             const int u = w - s;
 #pragma unroll
-            for (int kk = 0; kk < kKS / 16; ++kk) {
-              const uint64_t ad = adb + (uint64_t)((s * kABlock * 2 + kk * 256) >> 4);
-              const uint64_t bd = bdb + (uint64_t)((u * kBBlock * 2 + kk * 256) >> 4);
+            for (int kk = 0; kk < kSteps; ++kk) {
+              const uint64_t ad = adb + (uint64_t)((s * kAPart + kk * 256) >> 4);
+              const uint64_t bd = bdb + (uint64_t)((u * kBPart + kk * 256) >> 4);
               const uint32_t acc = (ks > 0 || s > 0 || kk > 0) ? 1u : 0u;
-              mma_bf16(acc_base + w * kTN, ad, bd, idesc, acc);
+              if (TF32)
+                mma_tf32(acc_base + w * kTN, ad, bd, idesc, acc);
+              else
+                mma_bf16(acc_base + w * kTN, ad, bd, idesc, acc);
             }
           }
         }
@@ -538,7 +659,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
       const uint32_t lane_base =
           tmem + b * kTmemCols + ((uint32_t)((warp - 4) * 32) << 16);
       P[(size_t)nt * (2 * Qp) + mt * kTM + row] =
-          tile_epilogue<NCLS>(lane_base, row, mt, nt, tiles, Ecol, tw, Qp);
+          tile_epilogue<FORM>(lane_base, row, mt, nt, tiles, Ecol, tw, Qp, nchc);
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
       if (lane == 0)
@@ -654,8 +775,9 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
   const int ntiles = (int)tiles.size();
   // Plan data cached per (q grid, rstep, chunk count): basis and twiddles.
   const cudaStream_t as = st->alloc_stream;
+  const bool tf32 = form_tf32(st->form);
   const bool same_grid = st->grid_K.size() == (size_t)nq && st->grid_rstep == rstep &&
-                         st->grid_nch >= nch_cap &&
+                         st->grid_nch >= nch_cap && st->grid_tf32 == tf32 &&
                          std::memcmp(st->grid_K.data(), h_K, sizeof(double) * nq) == 0;
   DBX_TRY(buf_grow(&st->W, (size_t)ntiles * kNSlab * kBSlabBytes, delta, as));
   DBX_TRY(buf_grow(&st->E, sizeof(int) * ntiles * kTN, delta, as));
@@ -667,17 +789,19 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
   DBX_TRY(buf_grow(&st->err, sizeof(int), delta, as));
   if (!same_grid) {
     DBX_TRY(buf_grow(&st->basis, (size_t)nrt * kNSlab * kASlabBytes, delta, as));
-    DBX_TRY(buf_grow(&st->twid, sizeof(float4) * (size_t)nch_cap * Qp, delta, as));
+    DBX_TRY(buf_grow(&st->twid, 2 * sizeof(float2) * (size_t)nch_cap * Qp, delta, as));
     const long long nb = 2LL * Qp * (kL / kRun);
-    basis_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, stream>>>(
+    auto bk = tf32 ? basis_kernel<true> : basis_kernel<false>;
+    bk<<<(unsigned)((nb + 255) / 256), 256, 0, stream>>>(
         d_K, nq, Qp, rstep, (__nv_bfloat16 *)st->basis.p);
     const long long nt2 = (long long)(nch_cap / kRun) * Qp;  // nch_cap: multiple of 64
     twiddle_kernel<<<(unsigned)((nt2 + 255) / 256), 256, 0, stream>>>(
-        d_K, nq, Qp, nch_cap, rstep, (float4 *)st->twid.p);
+        d_K, nq, Qp, nch_cap, rstep, (float2 *)st->twid.p);
     DBX_CUDA_TRY(cudaGetLastError());
     st->grid_K.assign(h_K, h_K + nq);
     st->grid_rstep = rstep;
     st->grid_nch = nch_cap;
+    st->grid_tf32 = tf32;
   }
   DBX_TRY(h2d_copy(st->tiles.p, tiles.data(), sizeof(TcTile) * ntiles, stream,
                    st->arena));
@@ -686,16 +810,15 @@ Error tc_prepare(TcState *st, std::vector<TcCol> cols,
                    stream, st->arena));
   st->h2d += sizeof(TcTile) * ntiles + sizeof(TcCol) * ncols + sizeof(int) * (nmodels + 1);
   if (!st->num_sms) {  // first use of this state: kernel attributes, SMs
-    DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<4>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kPSmemBytes));
-    DBX_CUDA_TRY(cudaFuncSetAttribute(gemm_persistent_kernel<2>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kPSmemBytes));
+    for (auto k : {gemm_persistent_kernel<kFormExact>, gemm_persistent_kernel<kFormBf16x3>,
+                   gemm_persistent_kernel<kFormTf32x3>})
+      DBX_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kPSmemBytes));
     int dev = 0;
     DBX_CUDA_TRY(cudaGetDevice(&dev));
     DBX_CUDA_TRY(cudaDeviceGetAttribute(&st->num_sms, cudaDevAttrMultiProcessorCount, dev));
   }
+  ++st->prep_gen;
   st->ncols = ncols;
   st->nmodels = nmodels;
   st->ntiles = ntiles;
@@ -716,17 +839,20 @@ Error tc_execute(TcState *st, const double *d_K, double *d_I,
   const long long nwarps = (long long)ntiles * kTN;
   long long kself = 0;  // first bin beyond the self distance
   while ((double)kself * st->rstep <= kSelfR) ++kself;
-  weights_kernel<<<(unsigned)((nwarps * 32 + 255) / 256), 256, 0, stream>>>(
+  auto wk = form_tf32(st->form) ? weights_kernel<true> : weights_kernel<false>;
+  wk<<<(unsigned)((nwarps * 32 + 255) / 256), 256, 0, stream>>>(
       (const TcTile *)st->tiles.p, ntiles, (const TcCol *)st->cols.p, kself,
       (__nv_bfloat16 *)st->W.p, (int *)st->E.p, (int *)st->nonself.p);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->start(DBX_T_DEBYE, stream);
   const int total = nrt * ntiles;
-  auto kern = st->classes == 2 ? gemm_persistent_kernel<2> : gemm_persistent_kernel<4>;
+  auto kern = st->form == kFormTf32x3   ? gemm_persistent_kernel<kFormTf32x3>
+              : st->form == kFormBf16x3 ? gemm_persistent_kernel<kFormBf16x3>
+                                        : gemm_persistent_kernel<kFormExact>;
   kern<<<std::min(total, st->num_sms), kPThreads, kPSmemBytes, stream>>>(
       (const __nv_bfloat16 *)st->basis.p, (const __nv_bfloat16 *)st->W.p,
-      (const TcTile *)st->tiles.p, (const int *)st->E.p, (const float4 *)st->twid.p,
-      Qp, nrt, ntiles, (double *)st->P.p, (int *)st->err.p);
+      (const TcTile *)st->tiles.p, (const int *)st->E.p, (const float2 *)st->twid.p,
+      Qp, st->grid_nch, nrt, ntiles, (double *)st->P.p, (int *)st->err.p);
   DBX_CUDA_TRY(cudaGetLastError());
   tm->stop(DBX_T_DEBYE, stream);
   dim3 rg((nq + 127) / 128, st->nmodels);

@@ -27,9 +27,15 @@ struct TcState {  // cached plan data (basis, twiddles) and workspace
   // shape of the prepared contraction
   int ncols = 0, nmodels = 0, ntiles = 0, nq = 0, Qp = 0;
   int num_sms = 0;  // persistent contraction: one CTA per SM
-  // weight classes accumulated: 4 = the exact split, 2 = the three-product
-  // (BF16x3) form used only to compare precisions
-  int classes = 4;
+  // operand form: 0 = the exact split (4 bf16 digits, 10 products); 1 =
+  // BF16x3 (2 digits, 3 products) and 2 = TF32x3 (2 tf32 parts, 3
+  // products), used only to compare precisions
+  int form = 0;
+  bool grid_tf32 = false;  // the cached basis is in the tf32 layout
+  // incremented by every tc_prepare: a caller that replays a prepared
+  // contraction (a captured graph) checks that nobody prepared another one
+  // on this state since
+  uint64_t prep_gen = 0;
   double rstep = 0;
   double *S_out = nullptr;  // optional: per-column row sums S[c][q]
   PinArena *arena = nullptr;            // staging of the descriptor uploads

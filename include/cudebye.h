@@ -71,6 +71,12 @@ typedef struct dbx_species {
                             per operand and three products (the BF16x3
                             scheme); not within 1e-6, for precision
                             comparisons only (dbx_intensity, dbx_pattern) */
+#define DBX_DEBYE_TF32 5 /* the tensor-core contraction with each operand
+                            split into tf32 hi/lo parts and three products
+                            (the TF32-split scheme), FP32 accumulation per
+                            256-bin chunk, FP64 chunk and q reduction; for
+                            precision comparisons only (dbx_intensity,
+                            dbx_pattern) */
 
 /* ---- context ---------------------------------------------------------- */
 

@@ -127,3 +127,30 @@ def test_plain_form(engine, orc):
     finally:
         for h in handles:
             h.free()
+
+
+def test_batch_replay_after_single_pattern_calls(engine):
+    """A single-pattern tensor-core call (dbx_pattern, also in the TF32 and
+    BF16x3 comparison forms) between two dbx_patterns calls on the same
+    models prepares the shared contraction state for another shape; the
+    second batch call must prepare again instead of replaying the stale
+    graph, and give the first call's numbers."""
+    mods = small_batch(48, n=4)
+    tt, K = mods[0].k_grid()
+    K = K[::9]
+    other = lattice.spinel(radius=11.0, target=1200, seed=49)
+    _, K2 = other.k_grid()
+    handles = [engine.upload(m.xyz, m.counts) for m in mods]
+    h2 = engine.upload(other.xyz, other.counts)
+    try:
+        nb = [m.nbins for m in mods]
+        I1 = engine.patterns(handles, 1e-3, nb, species_of(mods), K)
+        for mode in ("tc", "tf32", "tc3"):
+            engine.pattern(h2, other.rstep, other.nbins, other.species, K2[::3],
+                           mode=mode)
+            I2 = engine.patterns(handles, 1e-3, nb, species_of(mods), K)
+            np.testing.assert_array_equal(I1, I2)
+    finally:
+        for h in handles:
+            h.free()
+        h2.free()

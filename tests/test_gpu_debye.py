@@ -140,3 +140,26 @@ def test_tc3_form_is_the_less_precise_study_form(engine, orc):
     assert rel.max() <= 1e-6
     assert rel3.max() >= rel.max()
     assert rel3.max() < 1e-2, rel3.max()
+
+
+def test_tf32_split_form(engine, orc):
+    """DBX_DEBYE_TF32 (each operand split into tf32 hi/lo parts, three
+    products with FP32 accumulation per 256-bin chunk, FP64 chunk and q
+    sums) against the FP64 oracle on the precision grid (2theta 5-150 deg,
+    0.7107 A): its max relative error is bounded by 2e-5 here, below the
+    BF16x3 form's (22 significant bits per operand against 16) and above
+    the exact split's."""
+    m = lattice.spinel(radius=16.0, target=4000, seed=22,
+                       grid=lattice.GRID_PRECISION)
+    tt, K = m.k_grid()
+    K = K[::8]
+    got32, want = _model_case(engine, orc, m, K, "tf32")
+    got3, _ = _model_case(engine, orc, m, K, "tc3")
+    got, _ = _model_case(engine, orc, m, K, "tc")
+    rel32 = np.abs(got32 - want) / np.abs(want)
+    rel3 = np.abs(got3 - want) / np.abs(want)
+    rel = np.abs(got - want) / np.abs(want)
+    assert np.all(np.isfinite(got32))
+    assert rel32.max() <= 2e-5, rel32.max()
+    assert rel32.max() < rel3.max(), (rel32.max(), rel3.max())
+    assert rel.max() <= rel32.max()

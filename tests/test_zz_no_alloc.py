@@ -92,9 +92,10 @@ def test_noalloc_edge_cases_match_oracle(engine, orc):
     m = lattice.spinel(radius=13.0, target=2100, seed=33, rstep=1e-4)
     s = starts(m.counts)
     xyzd = device_xyz(torch, m.xyz)
-    # odd nbins over three windows (the last one ends on a low half)
-    nb_odd = 2 * 114688 + 1001
-    assert nb_odd % 2 == 1
+    # odd nbins over three windows (the last one ends on a low half), past
+    # the model's largest distance
+    nb_odd = m.nbins | 1
+    assert nb_odd % 2 == 1 and 2 * 114688 < nb_odd <= 3 * 114688
     rc, got = call(engine, torch, xyzd, s[0], m.counts[0], s[2], m.counts[2],
                    1e-4, nb_odd)
     want, bad = orc.block_histogram(m.xyz, s[0], m.counts[0], s[2],
