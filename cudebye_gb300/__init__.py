@@ -51,7 +51,7 @@ EXPORTS = (
     "dbx_k_grid", "dbx_atomic_prop", "dbx_intensity", "dbx_pattern",
     "dbx_set_stream", "dbx_set_timing", "dbx_get_timing", "dbx_get_traffic",
     "dbx_run_deb", "dbx_pair_histogram_noalloc", "dbx_patterns",
-    "dbx_pattern_errors",
+    "dbx_pattern_errors", "dbx_batch_tuning",
     "dbx_set_graphs", "dbx_server_create", "dbx_server_submit",
     "dbx_server_wait", "dbx_server_stats", "dbx_server_destroy",
     "dbx_check_sqrt", "dbx_xyz2deb", "dbx_xyz2deb_defaults", "dbx_deb_pack",
@@ -179,6 +179,7 @@ def load_library(path=None):
                                               ctypes.c_int, dp, ctypes.c_int,
                                               dp]),
         "dbx_set_graphs": (ctypes.c_int, [c_p, ctypes.c_int]),
+        "dbx_batch_tuning": (ctypes.c_int, [c_p, dp]),
         "dbx_check_sqrt": (ctypes.c_int, [c_p, ctypes.c_uint32, ctypes.c_uint32,
                                           i64p]),
         "dbx_server_create": (ctypes.c_int, [ctypes.POINTER(c_p), ctypes.c_int,
@@ -488,6 +489,17 @@ class Engine:
             self.ctx, model.id, rstep, nbins, sp, _ptr(K, ctypes.c_double),
             K.size, MODES[mode], _ptr(out, ctypes.c_double)))
         return out
+
+    def batch_tuning(self):
+        """The batch autotuner's choice for the last patterns() plan
+        (dbx_batch_tuning)."""
+        out = np.zeros(8)
+        self._check(self.lib.dbx_batch_tuning(self.ctx, _ptr(out, ctypes.c_double)))
+        return {"tasks": int(out[0]), "tasks_per_sm": float(out[1]),
+                "multi_window": bool(out[2]), "rowq": float(out[3]),
+                "geometry": ("sampled", "disjoint", "overlap")[int(out[4])],
+                "shapes_timed": int(out[5]), "task_counts_timed": int(out[6]),
+                "hist_ms": float(out[7])}
 
     def patterns(self, models, rstep, nbins, species, K, mode="tc", out=None):
         """Full patterns of several resident models in one pass

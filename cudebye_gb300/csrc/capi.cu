@@ -38,6 +38,12 @@ struct BatchState {
   cudaGraphExec_t exec = nullptr;
   std::vector<const void *> graph_ptrs;  // buffers the graph was built on
   int tuned_tasks = 0;
+  struct Tune {  // the autotuner's choice for this batch (dbx_batch_tuning)
+    int tasks = 0, geom = 0, shapes = 0, task_counts = 0;
+    double rowq = 0;
+    bool multi = false;
+    float ms = 0;
+  } tune;
   uint64_t tc_gen = 0;  // the contraction state's preparation of this batch
   bool valid = false;
 };
@@ -311,45 +317,131 @@ Error batch_device_pass(dbx_ctx *c, dbx::Timers *tm) {
                          c->stream, tm);
 }
 
-// Time the histogram of the batch plan for a few task granularities and
-// keep the fastest (tasks per SM).
-Error autotune_tasks(dbx_ctx *c) {
+// The histogram plan of a batch: every (model, species pair), with the
+// plan's shape policy (window geometry, 32-row items) as set in b.hp.plan.
+Error batch_plan(dbx_ctx *c, const std::vector<dbx::Model *> &ms, double rstep,
+                 const int64_t *nbins, int tasks) {
   BatchState &b = c->batch;
-  const int cand[3] = {4, 8, 16};
-  float best = 1e30f;
-  int best_t = c->hist_tasks;
-  cudaEvent_t e0, e1;
-  DBX_CUDA_TRY(cudaEventCreate(&e0));
-  DBX_CUDA_TRY(cudaEventCreate(&e1));
-  dbx::Timers off;
-  for (int t : cand) {
-    const int tasks = t * c->num_sms;
-    dbx::hist_plan_tasks(&b.hp.plan, tasks);
-    size_t delta = 0;
-    Error e = dbx::hist_upload(b.hp.plan, &b.hp.lists, c->stream, &delta);
-    c->used += delta;
-    if (e.code) return e;
-    cudaEventRecord(e0, c->stream);
-    e = dbx::hist_launch(b.hp.plan, b.hp.lists, &c->hws, (float)(1.0 / b.rstep),
-                         c->stream, c->num_sms, &delta, &off);
-    c->used += delta;
-    if (e.code) return e;
-    cudaEventRecord(e1, c->stream);
-    DBX_CUDA_TRY(cudaEventSynchronize(e1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best) {
-      best = ms;
-      best_t = tasks;
-    }
+  dbx::hist_plan_clear(&b.hp.plan);
+  for (size_t i = 0; i < ms.size(); ++i) {
+    dbx::Model *m = ms[i];
+    std::vector<int2> pairs;
+    for (int r = 0; r < m->nspecies; ++r)
+      for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
+    if (nbins[i] > dbx::hist_window_bins()) DBX_TRY(dbx::model_host_boxes(m, c->stream));
+    DBX_TRY(dbx::hist_plan_add(*m, pairs, rstep, nbins[i], m->d_hist, m->hist_pitch,
+                               &b.hp.plan));
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  b.tuned_tasks = best_t;
-  dbx::hist_plan_tasks(&b.hp.plan, best_t);
+  dbx::hist_plan_tasks(&b.hp.plan, tasks);
   size_t delta = 0;
   Error e = dbx::hist_upload(b.hp.plan, &b.hp.lists, c->stream, &delta);
   c->used += delta;
+  return e;
+}
+
+// Device time of one histogram launch of the uploaded batch plan.
+Error time_batch_hist(dbx_ctx *c, cudaEvent_t e0, cudaEvent_t e1, float *ms) {
+  BatchState &b = c->batch;
+  dbx::Timers off;
+  size_t delta = 0;
+  cudaEventRecord(e0, c->stream);
+  Error e = dbx::hist_launch(b.hp.plan, b.hp.lists, &c->hws, (float)(1.0 / b.rstep),
+                             c->stream, c->num_sms, &delta, &off);
+  c->used += delta;
+  if (e.code) return e;
+  cudaEventRecord(e1, c->stream);
+  DBX_CUDA_TRY(cudaEventSynchronize(e1));
+  cudaEventElapsedTime(ms, e0, e1);
+  return dbx::ok();
+}
+
+// The batch autotuner: times the histogram launch of the batch plan for
+// each candidate shape and keeps the fastest. Candidates: when the plan
+// splits histograms into several windows, the tile shape (32-row items
+// where they list fewer pairs, or 128-row items only) and the window
+// geometry (chosen per species pair from sampled tile pairs, or disjoint
+// windows only); then the CTA task count ({4, 8, 16} x SMs) of the chosen
+// shape. Every candidate gives the same histograms (integer sums).
+Error autotune(dbx_ctx *c, const std::vector<dbx::Model *> &ms, double rstep,
+               const int64_t *nbins) {
+  BatchState &b = c->batch;
+  dbx::HistPlan &plan = b.hp.plan;
+  cudaEvent_t e0, e1;
+  DBX_CUDA_TRY(cudaEventCreate(&e0));
+  DBX_CUDA_TRY(cudaEventCreate(&e1));
+  struct Ev {
+    cudaEvent_t a, b;
+    ~Ev() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } ev{e0, e1};
+  bool multi = false;
+  for (const dbx::HistSeg &sg : plan.segs) multi |= sg.shape == dbx::kSegList;
+  const int base_tasks = (multi ? 8 : 4) * c->num_sms;
+  b.tune = BatchState::Tune{};
+  float best = 1e30f;
+  int best_geom = dbx::kGeomSampled;
+  double best_rowq = dbx::hist_rowq_default();
+  if (multi) {
+    struct Shape {
+      int geom;
+      double rowq;
+    };
+    const double rq = dbx::hist_rowq_default();
+    const Shape cand[3] = {{dbx::kGeomSampled, rq},
+                           {dbx::kGeomSampled, 0.0},
+                           {dbx::kGeomDisjoint, rq}};
+    for (const Shape &sh : cand) {
+      plan.geom = sh.geom;
+      plan.rowq = sh.rowq;
+      DBX_TRY(batch_plan(c, ms, rstep, nbins, base_tasks));
+      float t0 = 0, t1 = 0;  // a warm launch, then the timed one
+      DBX_TRY(time_batch_hist(c, e0, e1, &t0));
+      DBX_TRY(time_batch_hist(c, e0, e1, &t1));
+      ++b.tune.shapes;
+      if (t1 < best) {
+        best = t1;
+        best_geom = sh.geom;
+        best_rowq = sh.rowq;
+      }
+    }
+    plan.geom = best_geom;
+    plan.rowq = best_rowq;
+    DBX_TRY(batch_plan(c, ms, rstep, nbins, base_tasks));
+  } else {
+    dbx::hist_plan_tasks(&plan, base_tasks);
+  }
+  best = 1e30f;
+  int best_t = base_tasks;
+  for (int t : {4, 8, 16}) {
+    const int tasks = t * c->num_sms;
+    dbx::hist_plan_tasks(&plan, tasks);
+    size_t delta = 0;
+    Error e = dbx::hist_upload(plan, &b.hp.lists, c->stream, &delta);
+    c->used += delta;
+    if (e.code) return e;
+    float ms_t = 0;
+    DBX_TRY(time_batch_hist(c, e0, e1, &ms_t));
+    ++b.tune.task_counts;
+    if (ms_t < best) {
+      best = ms_t;
+      best_t = tasks;
+    }
+  }
+  b.tuned_tasks = best_t;
+  b.tune.tasks = best_t;
+  b.tune.geom = best_geom;
+  b.tune.rowq = best_rowq;
+  b.tune.multi = multi;
+  b.tune.ms = best;
+  dbx::hist_plan_tasks(&plan, best_t);
+  size_t delta = 0;
+  Error e = dbx::hist_upload(plan, &b.hp.lists, c->stream, &delta);
+  c->used += delta;
+  // later plans start from the default shape again
+  plan.geom = dbx::kGeomSampled;
+  plan.rowq = dbx::hist_rowq_default();
   return e;
 }
 
@@ -381,18 +473,11 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
     b.hist_ptrs = hist_ptrs;
     b.rstep = rstep;
     b.K.assign(K, K + nq);
-    // one plan over every (model, pair)
-    dbx::hist_plan_clear(&b.hp.plan);
-    for (int i = 0; i < nm; ++i) {
-      dbx::Model *m = ms[i];
-      std::vector<int2> pairs;
-      for (int r = 0; r < m->nspecies; ++r)
-        for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
-      if (nbins[i] > dbx::hist_window_bins())
-        DBX_TRY(dbx::model_host_boxes(m, c->stream));
-      DBX_TRY(dbx::hist_plan_add(*m, pairs, rstep, nbins[i], m->d_hist,
-                                 m->hist_pitch, &b.hp.plan));
-    }
+    // one plan over every (model, pair), default shape; the autotuner
+    // below may re-plan it with another
+    b.hp.plan.geom = dbx::kGeomSampled;
+    b.hp.plan.rowq = dbx::hist_rowq_default();
+    DBX_TRY(batch_plan(c, ms, rstep, nbins, c->hist_tasks));
     // columns (model, pair) for the prefactor and the contraction
     b.model_col_begin.assign(1, 0);
     b.col_sp.clear();
@@ -431,7 +516,7 @@ Error patterns_tc(dbx_ctx *c, const std::vector<dbx::Model *> &ms,
     c->used += delta;
     delta = 0;
     if (e.code) return e;
-    DBX_TRY(autotune_tasks(c));
+    DBX_TRY(autotune(c, ms, rstep, nbins));
     DBX_TRY(dbx::hist_scratch(b.hp.plan, &c->hws, &delta));
     c->used += delta;
     delta = 0;
@@ -898,6 +983,20 @@ int dbx_pattern_errors(dbx_ctx *c, const int64_t *ids, int nmodels, double rstep
     sp0 += m->nspecies;
   }
   return DBX_OK;
+}
+
+int dbx_batch_tuning(const dbx_ctx *c, double out[8]) {
+  if (!c || !out) return DBX_ERR_ARG;
+  const BatchState::Tune &t = c->batch.tune;
+  out[0] = t.tasks;
+  out[1] = c->num_sms ? (double)t.tasks / c->num_sms : 0.0;
+  out[2] = t.multi ? 1.0 : 0.0;
+  out[3] = t.rowq;
+  out[4] = t.geom;
+  out[5] = t.shapes;
+  out[6] = t.task_counts;
+  out[7] = t.ms;
+  return c->batch.valid ? DBX_OK : DBX_ERR_ARG;
 }
 
 int dbx_set_graphs(dbx_ctx *c, int enable) {

@@ -116,7 +116,7 @@ struct Model {
                                             // sorted models filled on demand)
   float4 *d_atoms = nullptr;                // natoms x (x, y, z, 0)
   int2 *d_tiles = nullptr;
-  TileBox *d_boxes = nullptr;               // per tile (device-sorted models)
+  TileBox *d_boxes = nullptr;               // per tile (device)
   size_t dev_bytes = 0;
   // Cached histogram plan of all pairs for (plan_rstep, plan_nbins): the
   // work lists depend only on the geometry and the binning.
@@ -168,6 +168,7 @@ inline int pair_index(int p, int row, int col) {
 struct HistSeg {  // one (model, pair, bin window) accumulated in smem
   const float4 *atoms;      // the model's atoms
   const int2 *tiles;        // the model's tiles
+  const TileBox *boxes;     // the model's tile boxes (device)
   unsigned long long *out;  // the pair's histogram, bin 0
   int kb;                   // first bin of the window
   int wl;                   // window length in bins
@@ -189,6 +190,9 @@ struct HistSeg {  // one (model, pair, bin window) accumulated in smem
 };
 constexpr int kSegList = 0, kSegRect = 1, kSegTri = 2;
 constexpr int kItemQ0Shift = 25, kItemQ1Shift = 27;
+// bit 29: a 32-row item (rows [32 rq, 32 rq + 32) of tile I, rq in bits
+// 30-31), listed in multi-window histograms only
+constexpr int kItemRowQShift = 29, kItemRqShift = 30;
 constexpr int kItemTileMask = (1 << 25) - 1;
 struct HistTask {  // one CTA-sized slice of a segment's tile pairs
   int seg;
@@ -199,6 +203,9 @@ struct HistRow {  // an output histogram to zero before a launch
   unsigned long long *out;
   long long len;
 };
+
+double hist_rowq_default();  // DBX_HIST_ROWQ, else the measured default
+constexpr int kGeomSampled = 0, kGeomDisjoint = 1, kGeomOverlap = 2;
 
 struct HistPlan {
   std::vector<int2> items;     // {tile I, tile J | (diag << 31)}
@@ -211,6 +218,14 @@ struct HistPlan {
   std::vector<HistRow> rows;
   int window = 0;              // largest window in bins
   int nrows = 0;               // output histograms
+  // 32-row items are listed in multi-window histograms where they cut an
+  // item's pairs by more than this factor (0: never); not reset by
+  // hist_plan_clear
+  double rowq = hist_rowq_default();
+  // window geometry of multi-window histograms: chosen per species pair
+  // from sampled tile pairs (kGeomSampled), or forced; not reset by
+  // hist_plan_clear
+  int geom = 0;
   int64_t pairs = 0;           // binned pairs (the reference's "Distances
                                // Expected" summed over the selected pairs)
   size_t upload_bytes() const {
@@ -232,7 +247,8 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks);
 // (device pointers null, out = nullptr: output rows are byte offsets), with
 // the model's atoms, tiles and histogram base filled in.
 void hist_plan_append(HistPlan *plan, const HistPlan &part, const float4 *atoms,
-                      const int2 *tiles, unsigned long long *out);
+                      const int2 *tiles, const TileBox *boxes,
+                      unsigned long long *out);
 // clear + add + tasks for one model
 Error hist_plan(const Model &m, const std::vector<int2> &pairs, double rstep,
                 int64_t nbins, unsigned long long *out, int64_t pitch,

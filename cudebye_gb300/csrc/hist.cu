@@ -60,23 +60,80 @@ __device__ __forceinline__ void wrap_fix(unsigned old, unsigned v, unsigned wl,
   }
 }
 
+// How the pair loop treats bins outside its window (kMode):
+//  kFull:     the window covers bins [0, nbins); a valid pair beyond it is
+//             out of range (clamped to the lane's out-of-range counter);
+//  kFullSafe: the same window, and the tile boxes show that no pair of the
+//             item can bin beyond it: no clamp;
+//  kMid:      a window that is not the histogram's last (the planner gives
+//             it an unreachable nbins): pairs beyond it belong to other
+//             windows, never to the range-error count, and are ignored;
+//  kGeneral:  the last window of a wider histogram: bins beyond nbins are
+//             range errors, other misses are ignored.
+constexpr int kFull = 0, kFullSafe = 1, kMid = 2, kGeneral = 3;
+
+// One pair's shared-memory add. Every pair makes exactly one shared
+// atomic, with no branch: its virtual bin e is the window bin when it hits,
+// else this lane's out-of-range counter vo (a valid pair beyond the
+// histogram) or ignore word vi (a pair outside a diagonal or partial tile,
+// or in another window). Lane-private spare words avoid same-address
+// serialisation; adds to ignore words are 0. Bins are carried as the raw
+// bits of the rounding float, u = e + base (base even, so u and e have the
+// same parity), and the window's shared address is pre-offset by base:
+// word address = sadj + 4 (u >> 1). Returns the word's old value (u is
+// updated to the virtual bin actually added to).
+template <int kMode>
+__device__ __forceinline__ unsigned pair_add(unsigned &u, bool valid, unsigned base,
+                                             unsigned sadj, unsigned wl, unsigned kb,
+                                             unsigned nbins, unsigned uo,
+                                             unsigned ui) {
+  bool ignore = false;
+  if (kMode == kFullSafe) {
+    u = valid ? u : ui;
+    ignore = !valid;
+  } else if (kMode == kFull) {
+    // bins >= wl all count as out of range: clamp them to vo
+    u = valid ? min(u, uo) : ui;
+    ignore = !valid;
+  } else if (kMode == kMid) {
+    const bool hit = valid && u - base < wl;
+    u = hit ? u : ui;
+    ignore = !hit;
+  } else {
+    const unsigned lk = u - base;
+    const bool oor = valid && lk + kb >= nbins;
+    const bool hit = valid && lk < wl;
+    u = hit ? u : (oor ? uo : ui);
+    ignore = !hit && !oor;
+  }
+  // 1 << (16 * (u & 1)): the shift count is taken mod 32
+  unsigned inc = __funnelshift_l(0u, 1u, u << 4);
+  if (ignore) inc = 0u;  // ignore words stay 0
+  unsigned old;
+  asm volatile("atom.shared.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "r"(sadj + ((u >> 1) << 2)), "r"(inc));
+  return old;
+}
+
+// Whether an add wrapped its half (rotate the added half to the top: by 16
+// for an even bin), and the compensation if it did.
+__device__ __forceinline__ void wrap_check(unsigned old, unsigned u, unsigned base,
+                                           unsigned wl, unsigned vend,
+                                           unsigned long long *gh,
+                                           unsigned long long *oor_total) {
+  const unsigned rot = u * 16u + 16u;
+  if (__funnelshift_l(old, old, rot) >= 0xFFFF0000u)
+    wrap_fix(old, u - base, wl, vend, gh, oor_total);
+}
+
 // The column-atom loop of one tile pair for one warp: lanes hold four row
 // atoms; each column atom is one warp-uniform 16-byte load serving four
 // pairs. kAllValid: a full 128 x 128 off-diagonal tile pair (no per-pair
-// validity test). kFullWindow: the window covers bins [0, nbins), so a
-// valid pair that misses it is out of range.
-//
-// Every pair makes exactly one shared atomic, with no branch: its virtual
-// bin e is the window bin when it hits, else this lane's out-of-range
-// counter vo (a valid pair beyond the histogram) or ignore word vi (a pair
-// outside a diagonal or partial tile, or in another window). Lane-private
-// spare words avoid same-address serialisation; adds to ignore words are
-// 0. Bins are carried as the raw bits of the rounding float, u = e + base
-// (base even, so u and e have the same parity), and the window's shared
-// address is pre-offset by base: word address = sadj + 4 (u >> 1). Whether
-// an add wrapped its half is read from the returned old value; one test of
-// the four old words' sign bits guards the rare compensation.
-template <bool kAllValid, bool kFullWindow>
+// validity test). Whether an add wrapped its half is read from the
+// returned old value; one test of the four old words' sign bits guards the
+// rare compensation.
+template <bool kAllValid, int kMode>
 __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
                                           int jend, const float (&x)[4],
                                           const float (&y)[4],
@@ -104,37 +161,48 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
     unsigned any = 0u;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const bool valid = kAllValid || j <= jlim[r];
-      bool ignore = false;
-      if (kFullWindow) {
-        // bins >= wl all count as out of range: clamp them to vo
-        u[r] = valid ? min(u[r], uo) : ui;
-        ignore = !valid;
-      } else {
-        const unsigned lk = u[r] - base;
-        const bool oor = valid && lk + kb >= nbins;
-        const bool hit = valid && lk < wl;
-        u[r] = hit ? u[r] : (oor ? uo : ui);
-        ignore = !hit && !oor;
-      }
-      // 1 << (16 * (u & 1)): the shift count is taken mod 32
-      unsigned inc = __funnelshift_l(0u, 1u, u[r] << 4);
-      if (ignore) inc = 0u;  // ignore words stay 0
-      asm volatile("atom.shared.add.u32 %0, [%1], %2;"
-                   : "=r"(old[r])
-                   : "r"(sadj + ((u[r] >> 1) << 2)), "r"(inc));
+      old[r] = pair_add<kMode>(u[r], kAllValid || j <= jlim[r], base, sadj, wl, kb,
+                               nbins, uo, ui);
       any |= old[r];
     }
     // A wrap returns a half at 0xFFFF, so its bit 15 is set: the filter
     // passes only when some counter of these words has reached 32768.
     if (any & 0x80008000u) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        // rotate the added half to the top (by 16 for an even bin)
-        const unsigned rot = u[r] * 16u + 16u;
-        if (__funnelshift_l(old[r], old[r], rot) >= 0xFFFF0000u)
-          wrap_fix(old[r], u[r] - base, wl, vend, gh, oor_total);
-      }
+      for (int r = 0; r < 4; ++r) wrap_check(old[r], u[r], base, wl, vend, gh, oor_total);
+    }
+  }
+}
+
+// The same for a 32-row item: each lane holds one row atom and pairs it
+// with two column atoms per step (the packed arithmetic's two halves), so
+// an item covers a quarter of the row tile's atoms. The last, odd column
+// of an item is paired with a repeat of itself that counts nothing.
+template <bool kAllValid, int kMode>
+__device__ __forceinline__ void pair_loop32(const float4 *__restrict__ bj, int jend,
+                                            float x, float y, float z, int jlim,
+                                            float inv, unsigned base, unsigned sadj,
+                                            unsigned wl, unsigned kb, unsigned nbins,
+                                            unsigned long long *gh, unsigned vo,
+                                            unsigned vi, unsigned vend,
+                                            unsigned long long *oor_total) {
+  const f2 X = pk(x, x), Y = pk(y, y), Z = pk(z, z);
+  const unsigned uo = vo + base, ui = vi + base;
+  const f2 ninv = pk(-inv, -inv);
+#pragma unroll 2
+  for (int j = 0; j < jend; j += 2) {
+    const float4 b0 = __ldg(&bj[j]);  // warp-uniform: broadcast
+    const float4 b1 = __ldg(&bj[kAllValid ? j + 1 : min(j + 1, jend - 1)]);
+    const f2 bx = pk(b0.x, b1.x), by = pk(b0.y, b1.y), bz = pk(b0.z, b1.z);
+    unsigned u[2], old[2];
+    bins2(X, Y, Z, bx, by, bz, ninv, 0u, u[0], u[1]);
+    old[0] = pair_add<kMode>(u[0], kAllValid || j <= jlim, base, sadj, wl, kb, nbins,
+                             uo, ui);
+    old[1] = pair_add<kMode>(u[1], kAllValid || (j + 1 <= jlim && j + 1 < jend), base,
+                             sadj, wl, kb, nbins, uo, ui);
+    if ((old[0] | old[1]) & 0x80008000u) {
+      wrap_check(old[0], u[0], base, wl, vend, gh, oor_total);
+      wrap_check(old[1], u[1], base, wl, vend, gh, oor_total);
     }
   }
 }
@@ -203,6 +271,8 @@ __global__ void __launch_bounds__(kHistThreads, 1)
     const unsigned nbins = sg.nbins;
     const unsigned base = 0x4B000000u + kb;
     const bool full_window = kb == 0 && wl >= nbins;
+    // a window before the histogram's last: its misses are never range errors
+    const bool mid_window = !full_window && nbins == 0xFFFFFFFFu;
     // The pairs this segment counts are its window's bins [own_lo, own_lo +
     // own_len) (the whole window unless overlapping windows share bins):
     // the pair loop sees that range as its window, by offsetting the base,
@@ -225,6 +295,28 @@ __global__ void __launch_bounds__(kHistThreads, 1)
       // columns [jb, je): the item's quarters of tile J
       const int jb = kQuarter * (int)((ix >> kItemQ0Shift) & 3u);
       const int je = min(TJ.y, kQuarter * (4 - (int)((ix >> kItemQ1Shift) & 3u)));
+      const float4 *bj = atoms + TJ.x + jb;
+      if ((ix >> kItemRowQShift) & 1u) {
+        // a 32-row item: rows [32 rq, 32 rq + 32) of tile I, one per lane
+        // (listed by the planner in multi-window histograms only)
+        const int pi = kQuarter * (int)(ix >> kItemRqShift) + lane;
+        const bool act = pi < TI.y;
+        const float4 a = __ldg(&atoms[TI.x + (act ? pi : 0)]);
+        const int jl = act ? (diag ? pi - jb : 0x7fffffff) : -1;
+        const bool av = !diag && pi - lane + kQuarter <= TI.y && ((je - jb) & 1) == 0;
+#define DBX_PAIR_LOOP32(AV, MODE)                                                   \
+  pair_loop32<AV, MODE>(bj, je - jb, a.x, a.y, a.z, jl, inv, pbase, sadj, pwl, pkb, \
+                        nbins, pgh, pvo, pvi, pvend, oor_total)
+        if (mid_window) {
+          if (av) DBX_PAIR_LOOP32(true, kMid);
+          else DBX_PAIR_LOOP32(false, kMid);
+        } else {
+          if (av) DBX_PAIR_LOOP32(true, kGeneral);
+          else DBX_PAIR_LOOP32(false, kGeneral);
+        }
+#undef DBX_PAIR_LOOP32
+        continue;
+      }
       float x[4], y[4], z[4];
       int jlim[4];
 #pragma unroll
@@ -239,23 +331,42 @@ __global__ void __launch_bounds__(kHistThreads, 1)
         // loop counts columns from jb
         jlim[r] = act ? (diag ? pi - jb : 0x7fffffff) : -1;
       }
-      const float4 *bj = atoms + TJ.x + jb;
       const bool all_valid = !diag && TI.y == kTile;  // warp-uniform
-      if (all_valid) {
-        if (full_window)
-          pair_loop<true, true>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
-                                nbins, pgh, pvo, pvi, pvend, oor_total);
-        else
-          pair_loop<true, false>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
-                                 nbins, pgh, pvo, pvi, pvend, oor_total);
-      } else {
-        if (full_window)
-          pair_loop<false, true>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
-                                 nbins, pgh, pvo, pvi, pvend, oor_total);
-        else
-          pair_loop<false, false>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb,
-                                  nbins, pgh, pvo, pvi, pvend, oor_total);
+      int mode = full_window ? kFull : (mid_window ? kMid : kGeneral);
+      if (full_window) {
+        // No pair of the item can bin at or beyond wl if the distance bound
+        // of the tile boxes stays below it. The bound is computed in FP32
+        // with a margin far above the rounding of both it and the pairs'
+        // distances; NaN or infinite boxes fail the test.
+        const TileBox *BI = sg.boxes + (ix & (unsigned)kItemTileMask);
+        const TileBox *BJ = sg.boxes + (it.y & 0x7fffffff);
+        float d2 = 0.f, all = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float g1 = fabsf(__ldg(&BJ->hi[c]) - __ldg(&BI->lo[c]));
+          const float g2 = fabsf(__ldg(&BI->hi[c]) - __ldg(&BJ->lo[c]));
+          const float g = fmaxf(g1, g2);
+          d2 = fmaf(g, g, d2);
+          all += g1 + g2;  // NaN or infinite if any box coordinate is
+        }
+        if (all - all == 0.f && sqrtf(d2) * inv * 1.000244f + 2.0f < (float)wl)
+          mode = kFullSafe;
       }
+#define DBX_PAIR_LOOP(AV, MODE)                                                   \
+  pair_loop<AV, MODE>(bj, je - jb, x, y, z, jlim, inv, pbase, sadj, pwl, pkb, nbins, \
+                      pgh, pvo, pvi, pvend, oor_total)
+      if (all_valid) {
+        if (mode == kFullSafe) DBX_PAIR_LOOP(true, kFullSafe);
+        else if (mode == kFull) DBX_PAIR_LOOP(true, kFull);
+        else if (mode == kMid) DBX_PAIR_LOOP(true, kMid);
+        else DBX_PAIR_LOOP(true, kGeneral);
+      } else {
+        if (mode == kFullSafe) DBX_PAIR_LOOP(false, kFullSafe);
+        else if (mode == kFull) DBX_PAIR_LOOP(false, kFull);
+        else if (mode == kMid) DBX_PAIR_LOOP(false, kMid);
+        else DBX_PAIR_LOOP(false, kGeneral);
+      }
+#undef DBX_PAIR_LOOP
     }
     __syncthreads();
     unsigned *dst = partial + (size_t)t * (size_t)words_per_task;
@@ -418,6 +529,28 @@ static int64_t item_pairs(int nI, int nJ, bool diag) {
   return diag ? (int64_t)nI * (nI + 1) / 2 : (int64_t)nI * nJ;
 }
 
+// Pairs (i, j) of rows [i0, i1) and columns [j0, j1) of a tile pair, with
+// j <= i on a diagonal tile.
+static int64_t sub_pairs(int i0, int i1, int j0, int j1, bool diag) {
+  if (i1 <= i0 || j1 <= j0) return 0;
+  if (!diag) return (int64_t)(i1 - i0) * (j1 - j0);
+  int64_t n = 0;
+  for (int i = i0; i < i1; ++i) n += std::max(0, std::min(j1, i + 1) - j0);
+  return n;
+}
+
+// Cost of a pair in a 32-row item against one in a 128-row item (one more
+// column load and the packing of two columns per two pairs, against one
+// load and packing per four): 32-row items are listed where they cut the
+// pairs of an item by more than this factor. DBX_HIST_ROWQ sets it (0: never).
+double hist_rowq_default() {
+  static const double f = [] {
+    const char *v = getenv("DBX_HIST_ROWQ");
+    return v ? std::max(0.0, atof(v)) : 1.12;
+  }();
+  return f;
+}
+
 // Host threads for listing tile pairs (the machine's cores, at most 32).
 static int plan_threads() {
   static const int n = [] {
@@ -455,6 +588,7 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
                 "histogram needs 1 <= nbins <= 4194304 (got " +
                     std::to_string(nbins) + ")");
   const int W = kWindowBins;
+  const double rowq = plan->rowq;
   plan->window = std::max(plan->window, (int)std::min<int64_t>(W, nbins));
   const int64_t nwin = (nbins + W - 1) / W;
   const double inv = 1.0 / rstep;
@@ -478,6 +612,8 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
         HistSeg s;
         s.atoms = m.d_atoms;
         s.tiles = m.d_tiles;
+      s.boxes = m.d_boxes;
+        s.boxes = m.d_boxes;
         s.out = row;
         s.kb = 0;
         s.wl = (int)nbins;
@@ -598,6 +734,8 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       }
       overlap = co < cd;
     }
+    if (plan->geom == kGeomDisjoint) overlap = false;
+    if (plan->geom == kGeomOverlap) overlap = true;
     const Geom &g = overlap ? go : gd;
     const std::vector<int64_t> &kbw = g.kbw, &wlw = g.wlw, &own = g.own;
     for (int64_t w = 1; w < nwin; ++w)
@@ -627,9 +765,14 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
           box_bins(BI, m.boxes[J], inv, &kmin, &kmax);
           // In an owned list the item runs only over the columns whose
           // quarters reach the window's owned bins (their bin ranges from
-          // the quarter boxes, computed on first use).
+          // the quarter boxes, computed on first use), or is split into
+          // 32-row items, each over the column quarters its row quarter
+          // reaches, where that lists fewer pairs by more than the 32-row
+          // loop's extra cost per pair.
           int64_t qk0[4], qk1[4];
           int nq = -1;
+          int64_t rk0[4][4], rk1[4][4];  // row quarter x column quarter
+          int nr = -1;
           assign(g, kmin, kmax, [&](int64_t l) {
             if (!(l & 1)) {
               put(l, it, np);
@@ -647,16 +790,61 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
               }
             }
             const int64_t w = l / 2, lo = own[w], hi = own[w + 1];
+            // the last window counts bins >= nbins
+            auto reach = [&](int64_t k0, int64_t k1) {
+              return k1 >= lo && (w == nwin - 1 || std::max<int64_t>(k0, 0) < hi);
+            };
             unsigned mask = 0;
-            for (int q = 0; q < nq; ++q)  // the last window counts bins >= nbins
-              if (qk1[q] >= lo && (w == nwin - 1 || std::max<int64_t>(qk0[q], 0) < hi))
-                mask |= 1u << q;
+            for (int q = 0; q < nq; ++q)
+              if (reach(qk0[q], qk1[q])) mask |= 1u << q;
             if (!mask) return;
             const int q0 = __builtin_ctz(mask), q1 = 32 - __builtin_clz(mask);
             const int jb = q0 * kQuarter, je = std::min(nJ, q1 * kQuarter);
-            const int2 itq = make_int2(I | (q0 << kItemQ0Shift) | ((4 - q1) << kItemQ1Shift), it.y);
             const int npq = diag ? (je - jb) * TI.y - (jb + je - 1) * (je - jb) / 2
                                  : (je - jb) * TI.y;
+            if (rowq > 0) {
+              if (nr < 0) {
+                nr = (TI.y + kQuarter - 1) / kQuarter;
+                for (int r = 0; r < nr; ++r)
+                  for (int q = 0; q < nq; ++q) {
+                    TileBox R, Q;
+                    for (int d = 0; d < 3; ++d) {
+                      R.lo[d] = BI.qlo[r][d];
+                      R.hi[d] = BI.qhi[r][d];
+                      Q.lo[d] = m.boxes[J].qlo[q][d];
+                      Q.hi[d] = m.boxes[J].qhi[q][d];
+                    }
+                    box_bins(R, Q, inv, &rk0[r][q], &rk1[r][q]);
+                  }
+              }
+              int2 its[4];
+              int nps[4];
+              int nit = 0;
+              int64_t sum = 0;
+              for (int r = 0; r < nr; ++r) {
+                unsigned rm = 0;
+                for (int q = 0; q < nq; ++q)
+                  if (reach(rk0[r][q], rk1[r][q])) rm |= 1u << q;
+                if (!rm) continue;
+                const int r0 = __builtin_ctz(rm), r1 = 32 - __builtin_clz(rm);
+                const int cb = r0 * kQuarter, ce = std::min(nJ, r1 * kQuarter);
+                const int np32 = (int)sub_pairs(r * kQuarter, std::min(TI.y, (r + 1) * kQuarter),
+                                                  cb, ce, diag);
+                if (np32 == 0) continue;
+                its[nit] = make_int2(
+                    (int)((unsigned)I | ((unsigned)r0 << kItemQ0Shift) |
+                          ((unsigned)(4 - r1) << kItemQ1Shift) | (1u << kItemRowQShift) |
+                          ((unsigned)r << kItemRqShift)),
+                    it.y);
+                nps[nit++] = np32;
+                sum += np32;
+              }
+              if ((double)sum * rowq < (double)npq) {
+                for (int k = 0; k < nit; ++k) put(l, its[k], nps[k]);
+                return;
+              }
+            }
+            const int2 itq = make_int2(I | (q0 << kItemQ0Shift) | ((4 - q1) << kItemQ1Shift), it.y);
             put(l, itq, npq);
           });
         }
@@ -716,6 +904,7 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
       HistSeg s;
       s.atoms = m.d_atoms;
       s.tiles = m.d_tiles;
+      s.boxes = m.d_boxes;
       s.out = row;
       s.kb = (int)kbw[w];
       s.wl = (int)wlw[w];
@@ -816,7 +1005,8 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
 }
 
 void hist_plan_append(HistPlan *plan, const HistPlan &part, const float4 *atoms,
-                      const int2 *tiles, unsigned long long *out) {
+                      const int2 *tiles, const TileBox *boxes,
+                      unsigned long long *out) {
   auto rebase = [&](unsigned long long *p) {
     return reinterpret_cast<unsigned long long *>(reinterpret_cast<uintptr_t>(out) +
                                                   reinterpret_cast<uintptr_t>(p));
@@ -829,6 +1019,7 @@ void hist_plan_append(HistPlan *plan, const HistPlan &part, const float4 *atoms,
     HistSeg s = part.segs[i];
     s.atoms = atoms;
     s.tiles = tiles;
+    s.boxes = boxes;
     s.out = rebase(s.out);
     plan->segs.push_back(s);
     int2 si = part.seg_items[i];

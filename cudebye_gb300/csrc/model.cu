@@ -216,25 +216,33 @@ Error buf_grow(DevBuf *b, size_t bytes, size_t *delta, cudaStream_t stream) {
 
 size_t model_upload_bytes(const Model &m) {
   return sizeof(float4) * std::max<int64_t>(m.natoms, 1) +
-         sizeof(int2) * std::max<size_t>(m.tiles.size(), 1);
+         (sizeof(int2) + sizeof(TileBox)) * std::max<size_t>(m.tiles.size(), 1);
 }
 
 Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
                       PinArena *arena) {
   const size_t abytes = sizeof(float4) * std::max<int64_t>(m->natoms, 1);
   const size_t tbytes = sizeof(int2) * std::max<size_t>(m->tiles.size(), 1);
+  // the tile boxes go to the device too: the histogram kernel reads them to
+  // skip the out-of-range clamp of tile pairs that cannot reach it
+  const size_t bbytes = sizeof(TileBox) * std::max<size_t>(m->tiles.size(), 1);
   // with a staging arena (a server lane) the arrays are allocated in the
   // stream's order, without waiting for other streams
   if (arena ? (cudaMallocAsync(&m->d_atoms, abytes, stream) != cudaSuccess ||
-               cudaMallocAsync(&m->d_tiles, tbytes, stream) != cudaSuccess)
+               cudaMallocAsync(&m->d_tiles, tbytes, stream) != cudaSuccess ||
+               cudaMallocAsync(&m->d_boxes, bbytes, stream) != cudaSuccess)
             : (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
-               cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess))
+               cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess ||
+               cudaMalloc(&m->d_boxes, bbytes) != cudaSuccess))
     return fail(DBX_ERR_NOMEM, "device allocation failed for model");
-  m->dev_bytes = abytes + tbytes;
+  m->dev_bytes = abytes + tbytes + bbytes;
   DBX_CUDA_TRY(cudaMemcpyAsync(m->d_atoms, atoms, abytes,
                                cudaMemcpyHostToDevice, stream));
   if (!m->tiles.empty())
     DBX_TRY(h2d_copy(m->d_tiles, m->tiles.data(), sizeof(int2) * m->tiles.size(),
+                     stream, arena));
+  if (m->boxes.size() == m->tiles.size() && !m->boxes.empty())
+    DBX_TRY(h2d_copy(m->d_boxes, m->boxes.data(), sizeof(TileBox) * m->boxes.size(),
                      stream, arena));
   return ok();
 }

@@ -307,7 +307,8 @@ Error launch_round(dbx_server *s, Lane &L, const std::vector<Req *> &batch) {
   for (Req *r : batch) {
     if (r->kind != kNew) continue;
     SModel &sm = s->models[r->model_out];
-    hist_plan_append(&L.plan, r->part, sm.m->d_atoms, sm.m->d_tiles, sm.m->d_hist);
+    hist_plan_append(&L.plan, r->part, sm.m->d_atoms, sm.m->d_tiles, sm.m->d_boxes,
+                     sm.m->d_hist);
     rstep = sm.rstep;
   }
   hist_plan_tasks(&L.plan, s->hist_tasks);

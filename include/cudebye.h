@@ -251,6 +251,17 @@ int dbx_pattern_errors(dbx_ctx *ctx, const int64_t *model_ids, int nmodels,
                        const double *K, int nq, const double *I, int q_stride,
                        double *out_maxrel);
 
+/* The choices the batch autotuner made for the last dbx_patterns plan (no
+ * counterpart in the reference, whose tiling is the user's .deb line 1,
+ * cuDebye-v15.cu:644 and :152-224): out[0] histogram CTA tasks, out[1] tasks
+ * per SM, out[2] 1 if the plan splits histograms into several bin windows,
+ * out[3] the 32-row item factor chosen (0: 128-row items only), out[4] the
+ * window geometry (0 chosen per species pair from sampled tile pairs, 1
+ * disjoint windows), out[5] shapes timed, out[6] task counts timed, out[7]
+ * the chosen histogram launch's device time in ms. DBX_ERR_ARG before the
+ * first dbx_patterns call. */
+int dbx_batch_tuning(const dbx_ctx *ctx, double out[8]);
+
 /* CUDA-graph replay of dbx_patterns (default on). */
 int dbx_set_graphs(dbx_ctx *ctx, int enable);
 

@@ -154,3 +154,46 @@ def test_batch_replay_after_single_pattern_calls(engine):
         for h in handles:
             h.free()
         h2.free()
+
+
+def test_autotuner_picks_shape_on_fine_bins(engine, orc):
+    """A batch binned at 1e-4 A splits every histogram into several
+    shared-memory windows: the batch autotuner times three tile-shape /
+    window-geometry candidates and three task counts (dbx_batch_tuning),
+    and the histograms of the plan it keeps equal the oracle's bin for bin.
+    A single-window batch times the task counts only."""
+    rng = np.random.default_rng(50)
+    mods = []
+    for i in range(3):
+        m = lattice.random_model(rng, 800, 2500, lattice.GRID_CU, "f%d" % i, 50)
+        m.rstep = 1e-4
+        mods.append(m)
+    tt, K = mods[0].k_grid()
+    K = K[::30]
+    handles = [engine.upload(m.xyz, m.counts) for m in mods]
+    try:
+        nb = [m.nbins for m in mods]
+        assert min(nb) > 114688
+        engine.patterns(handles, 1e-4, nb, species_of(mods), K)
+        t = engine.batch_tuning()
+        assert t["multi_window"] and t["shapes_timed"] == 3
+        assert t["task_counts_timed"] == 3 and t["tasks"] > 0 and t["hist_ms"] > 0
+        assert t["geometry"] in ("sampled", "disjoint") and t["rowq"] >= 0
+        for m, h in zip(mods, handles):
+            got = engine.histogram(h, 1e-4, m.nbins)  # resident after the pass
+            want, bad = orc.model_histograms(m.xyz, m.counts, 1e-4, m.nbins)
+            assert bad == 0
+            np.testing.assert_array_equal(got, want)
+        one = small_batch(51, n=2)
+        h1 = [engine.upload(m.xyz, m.counts) for m in one]
+        try:
+            engine.patterns(h1, 1e-3, [m.nbins for m in one], species_of(one), K)
+            t1 = engine.batch_tuning()
+            assert not t1["multi_window"] and t1["shapes_timed"] == 0
+            assert t1["task_counts_timed"] == 3
+        finally:
+            for h in h1:
+                h.free()
+    finally:
+        for h in handles:
+            h.free()

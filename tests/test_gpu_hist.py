@@ -65,6 +65,40 @@ def test_fine_bins_many_windows(engine, orc, rstep):
     assert int(h.sum()) == m.pairs
 
 
+ROWQ = r"""
+import numpy as np, sys
+sys.path.insert(0, %r)
+import cudebye_gb300 as cd
+from cudebye_gb300 import lattice
+from oracle import pyoracle as orc
+for radius, target, seed, rstep in ((30.0, 25000, 13, 1.5e-4), (14.0, 1500, 11, 1e-4)):
+    m = lattice.spinel(radius=radius, target=target, seed=seed, rstep=rstep)
+    nbins = cd.channels(m.rmax, rstep)
+    with cd.Engine(0) as e:
+        mod = e.upload(m.xyz, m.counts)
+        got = e.histogram(mod, rstep, nbins)
+        one = e.split_calc_dist(mod, 1, 1, rstep, nbins)
+    want, bad = orc.model_histograms(m.xyz, m.counts, rstep, nbins)
+    assert bad == 0
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(one, want[len(m.counts)])
+print("OK")
+"""
+
+
+@pytest.mark.parametrize("factor", ["0", "0.01"])
+def test_row_quarter_items(orc, factor):
+    """Multi-window histograms with the 32-row item shape never used
+    (DBX_HIST_ROWQ=0: 128-row items over column quarters only) and used
+    wherever it lists fewer pairs (0.01), in child processes: every bin
+    equals the oracle's, including diagonal and ragged tiles."""
+    code = ROWQ % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, DBX_HIST_ROWQ=factor)
+    r = subprocess.run(["python", "-c", code], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
 def test_single_pair_entry_point(engine, orc):
     m = lattice.spinel(radius=12.0, target=1200, seed=12)
     mod = engine.upload(m.xyz, m.counts)
