@@ -428,20 +428,38 @@ constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
 // Epilogue of one tile for TMEM lane `row` (0..127) of accumulator set at
 // column offset acc_col: D = acc0 + acc1 2^-8 + acc2 2^-16 + acc3 2^-24,
 // scaled, rotated by the chunk twiddle and summed over the tile's 64 chunks.
-template <int FORM>
-__device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
-                                                int mt, int nt,
-                                                const TcTile *__restrict__ tiles,
-                                                const int *__restrict__ Ecol,
-                                                const float2 *__restrict__ tw,
-                                                int Qp, int nchc) {
-  const TcTile tile = tiles[nt];
+// The twiddle loads are the epilogue's long-latency step: the first group's
+// 16 are issued before the thread waits for the tile's accumulators
+// (epi_start), and each next group's while the current one is summed. The
+// chunks' scale exponents are read once per tile, two per lane, and passed
+// around by shuffles.
+struct EpiTile {
+  const float2 *twq;  // this row's twiddle plane, at chunk 0 of the grid
+  int ch0;            // the tile's first chunk
+  int e_lo, e_hi;     // scale exponents of chunks lane and lane + 32
+  float2 t[16];       // twiddles of the next group to sum
+};
+
+__device__ __forceinline__ void epi_start(EpiTile &et, int row, int mt, int nt,
+                                          const TcTile *__restrict__ tiles,
+                                          const int *__restrict__ Ecol,
+                                          const float2 *__restrict__ tw, int Qp,
+                                          int nchc, int lane) {
   const int m = mt * kTM + row;
   const bool sinrow = m >= Qp;
   const int q = sinrow ? m - Qp : m;
   // cosine rows are rotated by sin(q k0 dr), sine rows by cos(q k0 dr)
-  const float2 *twq = tw + (sinrow ? (size_t)nchc * Qp : 0) + q;
-  const int *E = Ecol + nt * kTN;
+  et.twq = tw + (sinrow ? (size_t)nchc * Qp : 0) + q;
+  et.ch0 = __ldg(&tiles[nt].ch0);
+  et.e_lo = __ldg(&Ecol[nt * kTN + lane]);
+  et.e_hi = __ldg(&Ecol[nt * kTN + 32 + lane]);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) et.t[i] = __ldg(&et.twq[(size_t)(et.ch0 + i) * Qp]);
+}
+
+template <int FORM>
+__device__ __forceinline__ double tile_epilogue(uint32_t lane_base, EpiTile &et,
+                                                int Qp) {
   constexpr int NCLS = form_classes(FORM);
   // weight of accumulator 1 against accumulator 0: one base-256 digit, or
   // none for the tf32 parts (hi*lo + lo*hi carry hi*hi's scale)
@@ -455,6 +473,14 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
     if (NCLS > 2) {
       tmem_ld16(lane_base + 2 * kTN + cg * 16, a2);
       tmem_ld16(lane_base + 3 * kTN + cg * 16, a3);
+    }
+    float2 tc[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) tc[i] = et.t[i];
+    if (cg + 1 < kTN / 16) {  // the next group's twiddles, in flight meanwhile
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        et.t[i] = __ldg(&et.twq[(size_t)(et.ch0 + (cg + 1) * 16 + i) * Qp]);
     }
     tmem_wait16(a0);
     tmem_wait16(a1);
@@ -473,13 +499,13 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, int row,
       const float lo = ((c0 - (hi - hb)) + (c1 - hb)) +
                        fmaf(__uint_as_float(a2[i]), 0x1p-16f,
                             __uint_as_float(a3[i]) * 0x1p-24f);
-      const float2 t = __ldg(&twq[(size_t)(tile.ch0 + n) * Qp]);
-      const float th = t.x, tl = t.y;
+      const float th = tc[i].x, tl = tc[i].y;
       // (th + tl) * (hi + lo) as a double-float, scaled by 2^(E-14)
       float p = th * hi;
       float pe = fmaf(th, hi, -p);
       pe = fmaf(th, lo, fmaf(tl, hi, pe));
-      const float sc = __int_as_float((__ldg(&E[n]) - 14 + 127) << 23);
+      const int e = __shfl_sync(0xffffffffu, n < 32 ? et.e_lo : et.e_hi, n & 31);
+      const float sc = __int_as_float((e - 14 + 127) << 23);
       p *= sc;
       pe *= sc;
       const float s = sh + p;
@@ -651,6 +677,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++tc) {
       const int b = tc & 1, ub = tc >> 1;
       const int mt = t % nrt, nt = t / nrt;
+      EpiTile et;  // the first twiddles load while the MMAs run
+      epi_start(et, row, mt, nt, tiles, Ecol, tw, Qp, nchc, lane);
       if (!mbar_wait(bar(ACCF + b), ub & 1)) {
         atomicExch(err, 1);
         break;
@@ -659,7 +687,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
       const uint32_t lane_base =
           tmem + b * kTmemCols + ((uint32_t)((warp - 4) * 32) << 16);
       P[(size_t)nt * (2 * Qp) + mt * kTM + row] =
-          tile_epilogue<FORM>(lane_base, row, mt, nt, tiles, Ecol, tw, Qp, nchc);
+          tile_epilogue<FORM>(lane_base, et, Qp);
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
       if (lane == 0)
