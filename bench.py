@@ -575,8 +575,12 @@ def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, seed=4,
                 out.append({"rate": rate, "submitted": nsub, "rescored": nres,
                             "failed_evicted": len(failed),
                             "patterns_per_s": len(lat) / span,
+                            "completed": len(lat),
                             "p50_ms": float(np.percentile(lat, 50)),
+                            "p90_ms": float(np.percentile(lat, 90)),
                             "p99_ms": float(np.percentile(lat, 99)),
+                            "p999_ms": float(np.percentile(lat, 99.9)),
+                            "max_ms": float(np.max(lat)),
                             "mean_atoms": float(np.mean(atoms)) if atoms else 0.0,
                             "max_arrival_lag_s": late,
                             "feed_wait_s": feed.waited_s - waited0})
