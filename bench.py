@@ -416,6 +416,21 @@ def io_bench(eng, nfiles=16, seed=8):
         out["run_deb_gamma_s"] = min(ts)
         out["reference_logged_gamma_s"] = {"load": 2.191, "compute_and_write": 11.563,
                                            "gpu": "GTX 980 Ti"}
+        # device phases of the Gamma pattern (3.56 M bins of 1e-4 A: the
+        # histogram in 31 shared-memory windows), CUDA events, median of 3
+        d = cd.read_deb(src)
+        _, Kg = cd.k_grid(d.lam, d.tt_min, d.tt_max, d.tt_step)
+        nbg = cd.channels(d.rmax, d.rstep)
+        mg = eng.upload(d.xyz, d.counts)
+        try:
+            ph = []
+            for _ in range(4):
+                eng.pattern(mg, d.rstep, nbg, d.species, Kg)
+                ph.append(eng.timing())
+        finally:
+            mg.free()
+        out["gamma_device_ms"] = {k: float(np.median([t[k] for t in ph[1:]]))
+                                  for k in ("hist", "hist_reduce", "debye")}
         d = os.path.join(tmp, "dir")
         os.mkdir(d)
         rng = np.random.default_rng(seed)
@@ -499,7 +514,7 @@ def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, seed=4,
     new request is a fresh spherical lattice model of 1,000-200,000 atoms
     (log-uniform, 1-4 species, random orientation and jitter) with its own
     2theta grid of 2,000-20,000 points, or, with probability 0.2, a
-    re-scoring of a resident model with new B factors. Latency = submit to
+    re-scoring of one of the 64 models completed last with new B factors. Latency = submit to
     result, measured by the server. The server admits by HBM footprint
     within `budget_gib`, evicting idle resident models; a re-score of a
     model evicted meanwhile fails with DBX_ERR_MODEL and is counted, not
@@ -518,7 +533,12 @@ def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, seed=4,
                 srv.wait(srv.submit(m.species, m.rstep, m.nbins, K, xyz=m.xyz,
                                     counts=m.counts), len(K))
             for rate in rates:
-                lat, done_t, resident, failed = [], [], [], []
+                # re-scores go to one of the 64 models completed last (a
+                # client re-scores what it has just seen; older ones may
+                # have been evicted under the HBM budget)
+                import collections
+                lat, done_t, failed = [], [], []
+                resident = collections.deque(maxlen=64)
                 lock = threading.Lock()
                 ex = cf.ThreadPoolExecutor(max_workers=64)
                 atoms = []
@@ -953,6 +973,9 @@ def run_engine(args):
         r = line["precision"]["results"]
         ns["precision_20000q_max_rel_err"] = {
             k: sig(r[k]["max_rel_err"], 2) for k in ("tc", "tf32", "tc3", "fp32")}
+    if "file_io" in line and "gamma_device_ms" in line["file_io"]:
+        ns["gamma_sample_device_ms"] = {
+            k: sig(v, 3) for k, v in line["file_io"]["gamma_device_ms"].items()}
     if "plain_small" in line:
         ns["plain_small"] = {"value": sig(line["plain_small"]["value"]),
                              "e2e": sig(line["plain_small"]["e2e"]["value"])}
