@@ -519,6 +519,7 @@ def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, seed=4,
     within `budget_gib`, evicting idle resident models; a re-score of a
     model evicted meanwhile fails with DBX_ERR_MODEL and is counted, not
     timed."""
+    import collections
     import concurrent.futures as cf
     import cudebye_gb300 as cd
     from cudebye_gb300 import lattice
@@ -536,7 +537,6 @@ def serving_bench(rates=(5, 20, 50, 100, 200, 400, 800), seconds=6.0, seed=4,
                 # re-scores go to one of the 64 models completed last (a
                 # client re-scores what it has just seen; older ones may
                 # have been evicted under the HBM budget)
-                import collections
                 lat, done_t, failed = [], [], []
                 resident = collections.deque(maxlen=64)
                 lock = threading.Lock()

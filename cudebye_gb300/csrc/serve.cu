@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -202,7 +203,13 @@ std::vector<Req *> admit(dbx_server *s) {
   int64_t round_pairs = 0;
   size_t pending = 0;                       // bytes of requests admitted now
   double round_rstep = 0;                   // new models of a round share it
-  const int64_t kMaxPairs = 40000000000LL;  // bounds a round's latency
+  // binned pairs of new models per round: bounds a round's device time,
+  // and so how long requests behind it wait (DBX_SERVE_ROUND_PAIRS)
+  static const int64_t kMaxPairs = [] {
+    const char *v = getenv("DBX_SERVE_ROUND_PAIRS");
+    const long long p = v ? atoll(v) : 0;
+    return p > 0 ? (int64_t)p : int64_t(40000000000LL);
+  }();
   for (auto it = s->queue.begin(); it != s->queue.end() && out.size() < 64;) {
     Req *r = *it;
     if (r->solo && !out.empty()) break;  // a retried request runs alone
