@@ -110,9 +110,12 @@ void release(dbx_ctx *c, dbx::DevBuf *b) {
   b->bytes = 0;
 }
 
+// The model's device arrays are freed in the context stream's order: work
+// queued on it before (an upload still copying) finishes first, and no
+// device-wide wait is made.
 void free_model(dbx_ctx *c, dbx::Model *m) {
   c->used -= dbx::model_device_bytes(*m);
-  dbx::model_release(m);
+  dbx::model_release_async(m, c->stream);
 }
 
 dbx::Model *find_model(dbx_ctx *c, int64_t id) {
@@ -147,13 +150,13 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   const int64_t pitch = pitch_of(nbins);
   const size_t bytes = sizeof(unsigned long long) * (size_t)pitch * np;
   if (m->hist_bytes < bytes) {
-    if (m->d_hist) cudaFree(m->d_hist);
+    if (m->d_hist) cudaFreeAsync(m->d_hist, c->stream);
     c->used -= m->hist_bytes;
     m->d_hist = nullptr;
     m->hist_bytes = 0;
     if (c->budget && c->used + bytes > c->budget)
       return dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by histograms");
-    DBX_CUDA_TRY(cudaMalloc(&m->d_hist, bytes));
+    DBX_CUDA_TRY(cudaMallocAsync(&m->d_hist, bytes, c->stream));
     m->hist_bytes = bytes;
     c->used += bytes;
   }
@@ -164,6 +167,9 @@ Error ensure_hist(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
       m->plan_cache = new dbx::HistPlanCache();
       m->plan_cache->lists.arena = &c->arena;
     }
+    // list buffers grow in the order of the stream the context uses now
+    // (dbx_set_stream may have changed it since the cache was made)
+    m->plan_cache->lists.alloc_stream = c->stream;
     std::vector<int2> pairs;
     for (int r = 0; r < m->nspecies; ++r)
       for (int q = r; q < m->nspecies; ++q) pairs.push_back(make_int2(r, q));
@@ -281,13 +287,13 @@ Error alloc_hist(dbx_ctx *c, dbx::Model *m, int64_t nbins) {
   const int64_t pitch = pitch_of(nbins);
   const size_t bytes = sizeof(unsigned long long) * (size_t)pitch * np;
   if (m->hist_bytes < bytes) {
-    if (m->d_hist) cudaFree(m->d_hist);
+    if (m->d_hist) cudaFreeAsync(m->d_hist, c->stream);
     c->used -= m->hist_bytes;
     m->d_hist = nullptr;
     m->hist_bytes = 0;
     if (c->budget && c->used + bytes > c->budget)
       return dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by histograms");
-    DBX_CUDA_TRY(cudaMalloc(&m->d_hist, bytes));
+    DBX_CUDA_TRY(cudaMallocAsync(&m->d_hist, bytes, c->stream));
     m->hist_bytes = bytes;
     c->used += bytes;
   }
@@ -784,7 +790,6 @@ int dbx_model_free(dbx_ctx *c, int64_t id) {
   auto it = c->models.find(id);
   if (it == c->models.end()) return DBX_ERR_MODEL;
   cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
   free_model(c, it->second.get());
   c->models.erase(it);
   return DBX_OK;

@@ -226,14 +226,11 @@ Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
   // the tile boxes go to the device too: the histogram kernel reads them to
   // skip the out-of-range clamp of tile pairs that cannot reach it
   const size_t bbytes = sizeof(TileBox) * std::max<size_t>(m->tiles.size(), 1);
-  // with a staging arena (a server lane) the arrays are allocated in the
-  // stream's order, without waiting for other streams
-  if (arena ? (cudaMallocAsync(&m->d_atoms, abytes, stream) != cudaSuccess ||
-               cudaMallocAsync(&m->d_tiles, tbytes, stream) != cudaSuccess ||
-               cudaMallocAsync(&m->d_boxes, bbytes, stream) != cudaSuccess)
-            : (cudaMalloc(&m->d_atoms, abytes) != cudaSuccess ||
-               cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess ||
-               cudaMalloc(&m->d_boxes, bbytes) != cudaSuccess))
+  // the arrays are allocated in the stream's order, without waiting for
+  // other work on the device
+  if (cudaMallocAsync(&m->d_atoms, abytes, stream) != cudaSuccess ||
+      cudaMallocAsync(&m->d_tiles, tbytes, stream) != cudaSuccess ||
+      cudaMallocAsync(&m->d_boxes, bbytes, stream) != cudaSuccess)
     return fail(DBX_ERR_NOMEM, "device allocation failed for model");
   m->dev_bytes = abytes + tbytes + bbytes;
   DBX_CUDA_TRY(cudaMemcpyAsync(m->d_atoms, atoms, abytes,
@@ -259,7 +256,15 @@ void model_release_async(Model *m, cudaStream_t stream) {
   m->d_tiles = nullptr;
   m->d_boxes = nullptr;
   m->d_hist = nullptr;
-  model_release(m);  // the plan cache, if any
+  if (m->plan_cache) {
+    for (DevBuf *b : {&m->plan_cache->lists.items, &m->plan_cache->lists.segs,
+                      &m->plan_cache->lists.tasks, &m->plan_cache->lists.rows})
+      if (b->p) {
+        cudaFreeAsync(b->p, stream);
+        b->p = nullptr;
+      }
+  }
+  model_release(m);  // the host part of the plan cache
 }
 
 void model_release(Model *m) {

@@ -321,9 +321,13 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
   A((void **)&lohi, sizeof(unsigned) * 6 * nspecies);
   A((void **)&d_start, sizeof(long long) * (nspecies + 1));
   A((void **)&d_bits, sizeof(int) * nspecies);
-  if (e == cudaSuccess && cudaMalloc(&m->d_atoms, abytes) != cudaSuccess) e = cudaErrorMemoryAllocation;
-  if (e == cudaSuccess && cudaMalloc(&m->d_tiles, tbytes) != cudaSuccess) e = cudaErrorMemoryAllocation;
-  if (e == cudaSuccess && cudaMalloc(&m->d_boxes, bbytes) != cudaSuccess) e = cudaErrorMemoryAllocation;
+  // the model's arrays in the stream's order too (no device-wide wait)
+  if (e == cudaSuccess && cudaMallocAsync(&m->d_atoms, abytes, st) != cudaSuccess)
+    e = cudaErrorMemoryAllocation;
+  if (e == cudaSuccess && cudaMallocAsync(&m->d_tiles, tbytes, st) != cudaSuccess)
+    e = cudaErrorMemoryAllocation;
+  if (e == cudaSuccess && cudaMallocAsync(&m->d_boxes, bbytes, st) != cudaSuccess)
+    e = cudaErrorMemoryAllocation;
   if (e != cudaSuccess) {
     cleanup();
     return fail(DBX_ERR_NOMEM, "device allocation failed for model");
