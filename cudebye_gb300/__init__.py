@@ -422,9 +422,8 @@ class Engine:
     def upload(self, xyz, counts):
         """Upload FP32 coordinates (n x 3, grouped by species in order)."""
         xyz = np.asarray(xyz, dtype=np.float32).reshape(-1, 3)
-        x = np.ascontiguousarray(xyz[:, 0])
-        y = np.ascontiguousarray(xyz[:, 1])
-        z = np.ascontiguousarray(xyz[:, 2])
+        t = np.ascontiguousarray(xyz.T)  # one pass: rows x, y, z (SoA)
+        x, y, z = t[0], t[1], t[2]
         c = np.ascontiguousarray(counts, dtype=np.int64)
         if int(c.sum()) != xyz.shape[0]:
             raise DebyeError(-6, "species counts do not sum to the atom count")
