@@ -150,7 +150,7 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
   const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
   const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
   const unsigned uo = vo + base, ui = vi + base;
-  const f2 ninv = pk(-inv, -inv);
+  const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
 #pragma unroll 2
   for (int j = 0; j < jend; ++j) {
     const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
@@ -188,7 +188,7 @@ __device__ __forceinline__ void pair_loop32(const float4 *__restrict__ bj, int j
                                             unsigned long long *oor_total) {
   const f2 X = pk(x, x), Y = pk(y, y), Z = pk(z, z);
   const unsigned uo = vo + base, ui = vi + base;
-  const f2 ninv = pk(-inv, -inv);
+  const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
 #pragma unroll 2
   for (int j = 0; j < jend; j += 2) {
     const float4 b0 = __ldg(&bj[j]);  // warp-uniform: broadcast

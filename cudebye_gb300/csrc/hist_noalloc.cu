@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned long long *gh = out + kb;
   const unsigned lim = nbins - (unsigned)kb;
   const unsigned base = 0x4B000000u + (unsigned)kb;
-  const f2 ninv = pk(-inv, -inv);
+  const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
   unsigned my_oor = 0;
   for (;;) {
     int idx = 0;

@@ -193,12 +193,23 @@ def _f32_directed(x64, toward):
 
 
 def _kernel_round_model(p):
-    """The kernel's roundf: floor(RZ(p + 0.5)) read from the bits of
-    RD(a + 2^23) (float32 operations emulated exactly in float64)."""
+    """The scalar kernel's roundf (bin_rel): floor(RZ(p + 0.5)) read from
+    the bits of RD(a + 2^23) (float32 operations emulated exactly in
+    float64)."""
     p = np.asarray(p, np.float32)
     a = _f32_directed(p.astype(np.float64) + 0.5, "z")
     t = _f32_directed(a.astype(np.float64) + 8388608.0, "d")
     return t.view(np.int32).astype(np.int64) - 0x4B000000
+
+
+def _kernel_round2_model(p):
+    """The tile kernels' roundf (bins2): q = 2p (exact), t = RD(q +
+    8388609), bin = (bits(t) >> 1) + 0x25800000 - bits(2^23)."""
+    p = np.asarray(p, np.float32)
+    q = (p.astype(np.float64) * 2.0).astype(np.float32)  # exact doubling
+    t = _f32_directed(q.astype(np.float64) + 8388609.0, "d")
+    bits = t.view(np.int32).astype(np.int64)
+    return (bits >> 1) + 0x25800000 - 0x4B000000
 
 
 def test_exact_roundf_without_conversion():
@@ -214,6 +225,28 @@ def test_exact_roundf_without_conversion():
     # roundf for p >= 0: half away from zero = floor(p + 0.5), exact in f64
     want = np.floor(p.astype(np.float64) + 0.5).astype(np.int64)
     np.testing.assert_array_equal(_kernel_round_model(p), want)
+    ok = p < np.float32(2 ** 22)  # beyond, every form lands out of range
+    np.testing.assert_array_equal(_kernel_round2_model(p)[ok], want[ok])
+
+
+def test_packed_roundf_every_float():
+    """The tile kernels' one-add roundf equals floor(p + 0.5) for every
+    float p in [0, 2^22), the bins any histogram can have; larger p give
+    bins of at least 2^22 (out of range for every histogram)."""
+    lo = int(np.float32(0).view(np.uint32))
+    hi = int(np.float32(2.0 ** 22).view(np.uint32))
+    step = 1 << 24
+    for start in range(lo, hi, step):
+        u = np.arange(start, min(start + step, hi), dtype=np.uint32)
+        p = u.view(np.float32).astype(np.float64)
+        q = 2.0 * p                       # exact
+        t = np.floor(q + 8388609.0)       # RD in [2^23, 2^24): the integers
+        t = np.where(q + 8388609.0 >= 2.0 ** 24,
+                     2.0 * np.floor((q + 8388609.0) / 2.0), t)  # spacing 2
+        got = np.floor((t - 8388608.0) / 2.0)
+        np.testing.assert_array_equal(got, np.floor(p + 0.5))
+    big = np.array([2.0 ** 22, 2.0 ** 23, 3e38], np.float32)
+    assert np.all(_kernel_round2_model(big) >= 2 ** 22)
 
 
 def test_packed_counter_bookkeeping():
