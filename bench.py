@@ -859,7 +859,8 @@ def run_engine(args):
     # operations per pair (3 sub, 3 mul, 2 add, square root as estimate + 4
     # correction ops, 1 mul, 2 for roundf), SMs x 128 FP32 lanes per clock.
     # Packed FP32x2 instructions do two of these per lane and issue slot, so
-    # a kernel can exceed this bound.
+    # a kernel can exceed this bound. (The tile kernels do roundf with one
+    # FP32 add and two integer operations; the bound keeps the formula's 16.)
     ops = 16
     peak = nsm * 128 * sm_mhz * 1e6 / ops / 1e9
     ach = m.pairs / (ph["hist"] / 1e3) / 1e9
