@@ -45,7 +45,8 @@ MODES = {"tc": 0, "fp64": 1, "fp32": 2, "plain": 3, "tc3": 4, "tf32": 5}
 # Every symbol include/cudebye.h declares (checked by the CPU tests).
 EXPORTS = (
     "dbx_create", "dbx_destroy", "dbx_strerror", "dbx_last_error",
-    "dbx_device_bytes", "dbx_model_upload", "dbx_model_free",
+    "dbx_device_bytes", "dbx_model_upload", "dbx_model_upload_xyz",
+    "dbx_model_free",
     "dbx_pair_histogram", "dbx_pair_histogram_plain", "dbx_histogram",
     "dbx_channels", "dbx_reduce_check",
     "dbx_k_grid", "dbx_atomic_prop", "dbx_intensity", "dbx_pattern",
@@ -135,6 +136,8 @@ def load_library(path=None):
         "dbx_device_bytes": (ctypes.c_size_t, [c_p]),
         "dbx_model_upload": (ctypes.c_int, [c_p, fp, fp, fp, i64p,
                                             ctypes.c_int, i64p]),
+        "dbx_model_upload_xyz": (ctypes.c_int, [c_p, fp, i64p, ctypes.c_int,
+                                                i64p]),
         "dbx_model_free": (ctypes.c_int, [c_p, ctypes.c_int64]),
         "dbx_pair_histogram": (ctypes.c_int, [c_p, ctypes.c_int64, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_double,
@@ -421,11 +424,23 @@ class Engine:
 
     def upload(self, xyz, counts):
         """Upload FP32 coordinates (n x 3, grouped by species in order)."""
-        xyz = np.asarray(xyz, dtype=np.float32).reshape(-1, 3)
-        t = np.ascontiguousarray(xyz.T)  # one pass: rows x, y, z (SoA)
-        x, y, z = t[0], t[1], t[2]
+        # interleaved [n][3] as given (dbx_model_upload_xyz): no transpose
+        xyz = np.ascontiguousarray(np.asarray(xyz, dtype=np.float32).reshape(-1, 3))
         c = np.ascontiguousarray(counts, dtype=np.int64)
         if int(c.sum()) != xyz.shape[0]:
+            raise DebyeError(-6, "species counts do not sum to the atom count")
+        mid = ctypes.c_int64()
+        self._check(self.lib.dbx_model_upload_xyz(
+            self.ctx, _ptr(xyz, ctypes.c_float), _ptr(c, ctypes.c_int64), len(c),
+            ctypes.byref(mid)))
+        return Model(self, mid.value, c)
+
+    def upload_planes(self, x, y, z, counts):
+        """Upload SoA coordinate planes (dbx_model_upload, the reference's
+        x[], y[], z[] arrays)."""
+        x, y, z = (np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z))
+        c = np.ascontiguousarray(counts, dtype=np.int64)
+        if not (x.size == y.size == z.size == int(c.sum())):
             raise DebyeError(-6, "species counts do not sum to the atom count")
         mid = ctypes.c_int64()
         self._check(self.lib.dbx_model_upload(

@@ -707,9 +707,13 @@ int dbx_destroy(dbx_ctx *c) {
   return DBX_OK;
 }
 
-int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
-                     const float *z, const int64_t *counts, int nspecies,
-                     int64_t *model_id) {
+namespace {
+
+// dbx_model_upload (x, y, z planes) and dbx_model_upload_xyz (xyz
+// interleaved [natoms][3]): exactly one of the two forms is given.
+int model_upload(dbx_ctx *c, const float *x, const float *y, const float *z,
+                 const float *xyz, const int64_t *counts, int nspecies,
+                 int64_t *model_id) {
   if (!c || !counts || nspecies < 1 || !model_id) return DBX_ERR_ARG;
   cudaSetDevice(c->device);
   auto m = std::make_unique<dbx::Model>();
@@ -747,7 +751,7 @@ int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
   Error e;
   for (int s = 0; s < nspecies; ++s)
     if (counts[s] < 0) return set_err(c, dbx::fail(DBX_ERR_ARG, "negative species count"));
-  if (natoms > 0 && (!x || !y || !z))
+  if (natoms > 0 && !xyz && (!x || !y || !z))
     return set_err(c, dbx::fail(DBX_ERR_ARG, "null coordinate array"));
   if (natoms >= (int64_t(1) << 31))
     return set_err(c, dbx::fail(DBX_ERR_ARG, "more than 2^31 atoms"));
@@ -757,9 +761,18 @@ int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
   if (c->budget && c->used + need > c->budget)
     return set_err(c, dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by model"));
   if (natoms >= dev_min) {
-    e = dbx::model_upload_sorted(m.get(), x, y, z, counts, nspecies, (float *)c->pin,
-                                 c->stream);
+    e = dbx::model_upload_sorted(m.get(), x, y, z, xyz, counts, nspecies,
+                                 (float *)c->pin, c->stream);
   } else {
+    std::vector<float> planes;  // small models: de-interleaved on the host
+    if (xyz) {
+      planes.resize(3 * (size_t)natoms);
+      for (int64_t i = 0; i < natoms; ++i)
+        for (int d = 0; d < 3; ++d) planes[d * natoms + i] = xyz[3 * i + d];
+      x = planes.data();
+      y = x + natoms;
+      z = y + natoms;
+    }
     e = dbx::model_prepare(x, y, z, counts, nspecies, m.get(), c->pin);
     if (e.code) return set_err(c, e);
     e = dbx::model_to_device(m.get(), c->pin, c->stream);
@@ -783,6 +796,22 @@ int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
   *model_id = m->id;
   c->models[m->id] = std::move(m);
   return DBX_OK;
+}
+
+}  // namespace
+
+int dbx_model_upload(dbx_ctx *c, const float *x, const float *y,
+                     const float *z, const int64_t *counts, int nspecies,
+                     int64_t *model_id) {
+  return model_upload(c, x, y, z, nullptr, counts, nspecies, model_id);
+}
+
+int dbx_model_upload_xyz(dbx_ctx *c, const float *xyz, const int64_t *counts,
+                         int nspecies, int64_t *model_id) {
+  int64_t natoms = 0;
+  for (int s = 0; counts && s < nspecies; ++s) natoms += std::max<int64_t>(counts[s], 0);
+  if (natoms > 0 && !xyz) return DBX_ERR_ARG;
+  return model_upload(c, nullptr, nullptr, nullptr, xyz, counts, nspecies, model_id);
 }
 
 int dbx_model_free(dbx_ctx *c, int64_t id) {

@@ -260,9 +260,20 @@ __global__ void tile_boxes_kernel(const float4 *__restrict__ atoms,
 
 }  // namespace
 
+// Interleaved coordinates [n][3] to the SoA planes x[], y[], z[] the sort
+// kernels read.
+__global__ void deinterleave_kernel(const float *__restrict__ aos, long long n,
+                                    float *__restrict__ soa) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  soa[i] = aos[3 * i];
+  soa[n + i] = aos[3 * i + 1];
+  soa[2 * n + i] = aos[3 * i + 2];
+}
+
 Error model_upload_sorted(Model *m, const float *x, const float *y, const float *z,
-                          const int64_t *counts, int nspecies, float *pin,
-                          cudaStream_t st) {
+                          const float *xyz, const int64_t *counts, int nspecies,
+                          float *pin, cudaStream_t st) {
   int64_t natoms = 0;
   for (int s = 0; s < nspecies; ++s) natoms += counts[s];
   const long long n = natoms;
@@ -292,20 +303,26 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
   const int ntiles = (int)m->tiles.size();
   const size_t abytes = sizeof(float4) * n, tbytes = sizeof(int2) * std::max(ntiles, 1),
                bbytes = sizeof(TileBox) * std::max(ntiles, 1);
-  // raw coordinates through the pinned staging (3n floats)
-  std::memcpy(pin, x, sizeof(float) * n);
-  std::memcpy(pin + n, y, sizeof(float) * n);
-  std::memcpy(pin + 2 * n, z, sizeof(float) * n);
+  // raw coordinates through the pinned staging (3n floats), as given: SoA
+  // planes, or one interleaved array de-interleaved on the device
+  if (xyz) {
+    std::memcpy(pin, xyz, sizeof(float) * 3 * n);
+  } else {
+    std::memcpy(pin, x, sizeof(float) * n);
+    std::memcpy(pin + n, y, sizeof(float) * n);
+    std::memcpy(pin + 2 * n, z, sizeof(float) * n);
+  }
   const long long nblk = (n + kSortChunk - 1) / kSortChunk;
-  float *d_xyz = nullptr;
+  float *d_xyz = nullptr, *d_aos = nullptr;
   unsigned long long *k1 = nullptr, *k2 = nullptr;
   int *i1 = nullptr, *i2 = nullptr;
   unsigned *cnt = nullptr, *lohi = nullptr;
   long long *d_start = nullptr;
   int *d_bits = nullptr;
   auto cleanup = [&] {
-    for (void *p : {(void *)d_xyz, (void *)k1, (void *)k2, (void *)i1, (void *)i2,
-                    (void *)cnt, (void *)lohi, (void *)d_start, (void *)d_bits})
+    for (void *p : {(void *)d_xyz, (void *)d_aos, (void *)k1, (void *)k2, (void *)i1,
+                    (void *)i2, (void *)cnt, (void *)lohi, (void *)d_start,
+                    (void *)d_bits})
       if (p) cudaFreeAsync(p, st);
   };
   cudaError_t e = cudaSuccess;
@@ -313,6 +330,7 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
     if (e == cudaSuccess) e = cudaMallocAsync(p, b, st);
   };
   A((void **)&d_xyz, sizeof(float) * 3 * n);
+  if (xyz) A((void **)&d_aos, sizeof(float) * 3 * n);
   A((void **)&k1, 8 * n);
   A((void **)&k2, 8 * n);
   A((void **)&i1, 4 * n);
@@ -339,7 +357,12 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
       lohi0[s * 6 + d] = 0xFFFFFFFFu;
       lohi0[s * 6 + 3 + d] = 0u;
     }
-  e = cudaMemcpyAsync(d_xyz, pin, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st);
+  e = cudaMemcpyAsync(xyz ? d_aos : d_xyz, pin, sizeof(float) * 3 * n,
+                      cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && xyz) {
+    deinterleave_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_aos, n, d_xyz);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(lohi, lohi0.data(), sizeof(unsigned) * lohi0.size(),
                         cudaMemcpyHostToDevice, st);

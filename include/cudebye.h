@@ -100,6 +100,13 @@ size_t dbx_device_bytes(const dbx_ctx *ctx);
 int dbx_model_upload(dbx_ctx *ctx, const float *x, const float *y,
                      const float *z, const int64_t *species_counts,
                      int nspecies, int64_t *model_id);
+/* The same for coordinates interleaved as xyz[natoms][3] (x0 y0 z0 x1 ...),
+ * the layout of .xyz files and of most host programs; no counterpart in the
+ * reference, whose reader fills separate x, y, z arrays. Large models are
+ * de-interleaved on the device, so the caller needs no transposed copy. */
+int dbx_model_upload_xyz(dbx_ctx *ctx, const float *xyz,
+                         const int64_t *species_counts, int nspecies,
+                         int64_t *model_id);
 int dbx_model_free(dbx_ctx *ctx, int64_t model_id);
 
 /* ---- hot path 1: distance histogram ----------------------------------- */

@@ -360,3 +360,24 @@ def test_device_sort_edge_cases():
     r = subprocess.run(["python", "-c", code], env=env, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
+def test_interleaved_and_planar_uploads_agree(engine, orc):
+    """dbx_model_upload_xyz (interleaved [n][3], de-interleaved on the host
+    for small models and on the device before the device sort for large
+    ones) and dbx_model_upload (x, y, z planes) give the same histograms,
+    and the oracle's."""
+    for m in (lattice.spinel(radius=14.0, target=2500, seed=61),
+              lattice.spinel(radius=34.0, target=60000, seed=62)):  # 42,735 atoms: device sort
+        h1 = engine.upload(m.xyz, m.counts)
+        h2 = engine.upload_planes(m.xyz[:, 0], m.xyz[:, 1], m.xyz[:, 2], m.counts)
+        try:
+            a = engine.histogram(h1, m.rstep, m.nbins)
+            b = engine.histogram(h2, m.rstep, m.nbins)
+        finally:
+            h1.free()
+            h2.free()
+        np.testing.assert_array_equal(a, b)
+        want, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins)
+        assert bad == 0
+        np.testing.assert_array_equal(a, want)
