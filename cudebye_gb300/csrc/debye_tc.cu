@@ -32,8 +32,13 @@
 // engine, cp.async.bulk) completing on an mbarrier. A persistent CTA per SM
 // runs three roles: a producer thread streams slabs through two stages, an
 // MMA thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> f32, M=128,
-// N=64, K=16) into one of two TMEM accumulator sets (4 classes x 64 f32
-// columns each) and commits, four epilogue warps drain the other set.
+// K=16) into one of two TMEM accumulator sets (4 classes x 64 f32 columns
+// each) and commits, four epilogue warps drain the other set. One MMA
+// multiplies digit s of A by all W digits t <= 3 - s at once (N = 256, 192,
+// 128, 64): W's digit blocks lie one after another along N, and the classes
+// one after another in TMEM, so product (s, t) lands in class s + t — four
+// MMAs per K step instead of ten, and A read from shared memory once per
+// digit.
 // Every wait is bounded and reports a timeout through an error word.
 //
 // Two comparison forms share the kernel: BF16x3 (two 8-bit digits per
@@ -605,11 +610,9 @@ __global__ void __launch_bounds__(kPThreads, 1)
     // MMA issuer
     constexpr int NCLS = form_classes(FORM);
     constexpr bool TF32 = form_tf32(FORM);
-    constexpr uint32_t idesc = make_idesc(kTM, kTN, TF32);
-    // bytes of one digit (part) block of A and W, and the MMA K step: 16
-    // bf16 or 8 tf32 elements, two core matrices (256 bytes) either way
+    // bytes of one digit (part) block of A, and the MMA K step: 16 bf16 or
+    // 8 tf32 elements, two core matrices (256 bytes) either way
     constexpr int kAPart = TF32 ? kABlock * 4 : kABlock * 2;
-    constexpr int kBPart = TF32 ? kBBlock * 4 : kBBlock * 2;
     constexpr int kSteps = TF32 ? kKS / 8 : kKS / 16;
     constexpr uint32_t kSbo = TF32 ? 2048 : 1024;
     int it = 0, tc = 0;
@@ -637,20 +640,22 @@ __global__ void __launch_bounds__(kPThreads, 1)
         // issuing thread limited the MMA rate)
         const uint64_t adb = make_desc(sA, 128, kSbo), bdb = make_desc(sB, 128, kSbo);
 #pragma unroll
-        for (int w = 0; w < NCLS; ++w) {
+        for (int s = 0; s < NCLS; ++s) {
+          // digit s of A against digits 0 .. NCLS-1-s of W in one MMA: the
+          // W digit blocks follow one another along N with the same 8-row
+          // stride, so N = (NCLS - s) * 64 columns read them all, and with
+          // D at class s the block of digit t lands in class s + t
+          const uint32_t idn = make_idesc(kTM, (NCLS - s) * kTN, TF32);
 #pragma unroll
-          for (int s = 0; s <= w; ++s) {
-            const int u = w - s;
-#pragma unroll
-            for (int kk = 0; kk < kSteps; ++kk) {
-              const uint64_t ad = adb + (uint64_t)((s * kAPart + kk * 256) >> 4);
-              const uint64_t bd = bdb + (uint64_t)((u * kBPart + kk * 256) >> 4);
-              const uint32_t acc = (ks > 0 || s > 0 || kk > 0) ? 1u : 0u;
-              if (TF32)
-                mma_tf32(acc_base + w * kTN, ad, bd, idesc, acc);
-              else
-                mma_bf16(acc_base + w * kTN, ad, bd, idesc, acc);
-            }
+          for (int kk = 0; kk < kSteps; ++kk) {
+            const uint64_t ad = adb + (uint64_t)((s * kAPart + kk * 256) >> 4);
+            const uint64_t bd = bdb + (uint64_t)((kk * 256) >> 4);
+            // the first MMA of a tile spans every class and starts them all
+            const uint32_t acc = (ks > 0 || s > 0 || kk > 0) ? 1u : 0u;
+            if (TF32)
+              mma_tf32(acc_base + s * kTN, ad, bd, idn, acc);
+            else
+              mma_bf16(acc_base + s * kTN, ad, bd, idn, acc);
           }
         }
         asm volatile(
