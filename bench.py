@@ -881,7 +881,8 @@ def run_engine(args):
     flops = 2.0 * len(K) * m.nbins * npair_types
     tc_ach = flops / (ph["debye"] / 1e3) / 1e12
     # bf16 MMA work the split form issues: per 128-row x 64-chunk x 256-bin
-    # tile, 10 digit-pair products of 2 x 128 x 64 x 256 FLOP
+    # tile, 10 digit-pair products of 2 x 128 x 64 x 256 FLOP (four MMAs of
+    # N = 256, 192, 128, 64 per K step)
     qp = (len(K) + 127) // 128 * 128
     nch = (m.nbins + 255) // 256  # 256-bin chunks per pair type
     col_tiles = npair_types * ((nch + 63) // 64)
@@ -898,7 +899,8 @@ def run_engine(args):
                "issued": {"achieved": issued_tf, "frac": issued_tf / pk["bf16_tflops"],
                           "unit": "TFLOP/s",
                           "basis": "bf16 MMA FLOP issued: 10 digit-pair products "
-                                   "per 128 x 64 x 256 tile, %d tiles" %
+                                   "per 128 x 64 x 256 tile (MMAs of N = 256, "
+                                   "192, 128, 64 per K step), %d tiles" %
                                    ((2 * qp // 128) * col_tiles)}}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws,

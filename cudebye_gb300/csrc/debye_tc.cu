@@ -87,19 +87,19 @@ constexpr int kFormTf32x3 = 2;  // 2 tf32 parts, 3 products
 __host__ __device__ constexpr int form_classes(int f) { return f == kFormExact ? 4 : 2; }
 __host__ __device__ constexpr bool form_tf32(int f) { return f == kFormTf32x3; }
 
-// Element offset of (row, k) inside a [rows x 64] block stored as 8x8
+// Element offset of (row, k) inside a [rows x kKS] block stored as 8x8
 // core matrices (8 rows x 16 bytes each, contiguous), row groups outermost:
-// core (g, kc) at (g*8 + kc)*64 elements. Leading (K) byte offset 128,
-// stride (row-group) byte offset 1024.
+// core (g, kc) at (g*kKS/8 + kc)*64 elements. Leading (K) byte offset 128,
+// stride (row-group) byte offset kKS*16.
 __host__ __device__ inline int tiled_off(int row, int k) {
-  return ((((row >> 3) << 3) + (k >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
+  return (((row >> 3) * (kKS / 8) + (k >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
 }
 
 // The same for 32-bit elements (8 rows x 4 elements per core matrix): core
-// (g, kc) at (g*16 + kc)*32 elements. Leading byte offset 128, stride
-// byte offset 2048.
+// (g, kc) at (g*kKS/4 + kc)*32 elements. Leading byte offset 128, stride
+// byte offset kKS*32.
 __host__ __device__ inline int tiled_off32(int row, int k) {
-  return ((((row >> 3) << 4) + (k >> 2)) << 5) + ((row & 7) << 2) + (k & 3);
+  return (((row >> 3) * (kKS / 4) + (k >> 2)) << 5) + ((row & 7) << 2) + (k & 3);
 }
 
 // Nearest tf32 (10 explicit mantissa bits; ties away from zero) of a
@@ -426,8 +426,8 @@ __device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
 // acce[b] (set b drained by the epilogue). Every wait is bounded; a role that
 // times out records the error and stops, and the others then time out too.
 constexpr int kPThreads = 256;
-constexpr int kPStages = 2;
 constexpr int kPStageBytes = kASlabBytes + kBSlabBytes;
+constexpr int kPStages = (192 * 1024) / kPStageBytes;  // 192 KB of stages
 constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
 
 // Epilogue of one tile for TMEM lane `row` (0..127) of accumulator set at
@@ -462,6 +462,17 @@ __device__ __forceinline__ void epi_start(EpiTile &et, int row, int mt, int nt,
   for (int i = 0; i < 16; ++i) et.t[i] = __ldg(&et.twq[(size_t)(et.ch0 + i) * Qp]);
 }
 
+// (h, l) += (p, pe): double-float accumulation with an exact two-sum of
+// the leading parts.
+__device__ __forceinline__ void dd_add(float &h, float &l, float p, float pe) {
+  const float s = h + p;
+  const float bb = s - h;
+  const float e2 = (h - (s - bb)) + (p - bb);
+  l += e2 + pe;
+  h = s + l;
+  l = l - (h - s);
+}
+
 template <int FORM>
 __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, EpiTile &et,
                                                 int Qp) {
@@ -469,7 +480,9 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, EpiTile &et,
   // weight of accumulator 1 against accumulator 0: one base-256 digit, or
   // none for the tf32 parts (hi*lo + lo*hi carry hi*hi's scale)
   constexpr float kC1 = form_tf32(FORM) ? 1.0f : 0x1p-8f;
-  float sh = 0.f, sl = 0.f;
+  // two running sums (even and odd chunks) halve the dependent chain of
+  // additions per tile; they are joined once at the end
+  float sh[2] = {0.f, 0.f}, sl[2] = {0.f, 0.f};
 #pragma unroll 1
   for (int cg = 0; cg < kTN / 16; ++cg) {
     uint32_t a0[16], a1[16], a2[16] = {}, a3[16] = {};
@@ -511,17 +524,11 @@ __device__ __forceinline__ double tile_epilogue(uint32_t lane_base, EpiTile &et,
       pe = fmaf(th, lo, fmaf(tl, hi, pe));
       const int e = __shfl_sync(0xffffffffu, n < 32 ? et.e_lo : et.e_hi, n & 31);
       const float sc = __int_as_float((e - 14 + 127) << 23);
-      p *= sc;
-      pe *= sc;
-      const float s = sh + p;
-      const float bb = s - sh;
-      const float e2 = (sh - (s - bb)) + (p - bb);
-      sl += e2 + pe;
-      sh = s + sl;
-      sl = sl - (sh - s);
+      dd_add(sh[i & 1], sl[i & 1], p * sc, pe * sc);
     }
   }
-  return (double)sh + (double)sl;
+  dd_add(sh[0], sl[0], sh[1], sl[1]);
+  return (double)sh[0] + (double)sl[0];
 }
 
 // FORM kFormExact: the exact form (digit pairs with s + t <= 3, four
@@ -614,7 +621,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
     // 8 tf32 elements, two core matrices (256 bytes) either way
     constexpr int kAPart = TF32 ? kABlock * 4 : kABlock * 2;
     constexpr int kSteps = TF32 ? kKS / 8 : kKS / 16;
-    constexpr uint32_t kSbo = TF32 ? 2048 : 1024;
+    constexpr uint32_t kSbo = TF32 ? kKS * 32 : kKS * 16;
     int it = 0, tc = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++tc) {
