@@ -83,10 +83,10 @@ constexpr int kFull = 0, kFullSafe = 1, kMid = 2, kGeneral = 3;
 // word address = sadj + 4 (u >> 1). Returns the word's old value (u is
 // updated to the virtual bin actually added to).
 template <int kMode>
-__device__ __forceinline__ unsigned pair_add(unsigned &u, bool valid, unsigned base,
-                                             unsigned sadj, unsigned wl, unsigned kb,
-                                             unsigned nbins, unsigned uo,
-                                             unsigned ui) {
+__device__ __forceinline__ unsigned pair_add_bin(unsigned &u, bool valid, unsigned base,
+                                                 unsigned sadj, unsigned wl, unsigned kb,
+                                                 unsigned nbins, unsigned uo,
+                                                 unsigned ui) {
   bool ignore = false;
   if (kMode == kFullSafe) {
     u = valid ? u : ui;
@@ -118,13 +118,80 @@ __device__ __forceinline__ unsigned pair_add(unsigned &u, bool valid, unsigned b
 
 // Whether an add wrapped its half (rotate the added half to the top: by 16
 // for an even bin), and the compensation if it did.
-__device__ __forceinline__ void wrap_check(unsigned old, unsigned u, unsigned base,
-                                           unsigned wl, unsigned vend,
-                                           unsigned long long *gh,
-                                           unsigned long long *oor_total) {
+__device__ __forceinline__ void wrap_check_bin(unsigned old, unsigned u, unsigned base,
+                                               unsigned wl, unsigned vend,
+                                               unsigned long long *gh,
+                                               unsigned long long *oor_total) {
   const unsigned rot = u * 16u + 16u;
   if (__funnelshift_l(old, old, rot) >= 0xFFFF0000u)
     wrap_fix(old, u - base, wl, vend, gh, oor_total);
+}
+
+// The raw form skips forming the bin: a pair is carried as the raw bits w
+// of its rounding float (bits2), w = bits(2^23) + 2 bin + r with r the
+// rounding bit. Its counter word is bin >> 1 = (w - bits(2^23)) >> 2 and
+// its half bin & 1 = bit 1 of w, so the shared address is sadjw + (w & ~3)
+// with sadjw = sadj + bits(2^23) (4 (u >> 1) = (w & ~3) + bits(2^23) for u
+// = bits(2^23) + bin), and a virtual bin v (a window bin or a spare word's
+// half, as wrap_fix numbers them) is w = wbase + 2 v, wbase = 2 base -
+// bits(2^23). Window tests hold on these values as on bins: for integers
+// b, n and r in {0, 1}, 2 b + r < 2 n exactly when b < n; NaN and infinite
+// distances have larger bits than any window value. One add, one mask and
+// a shift pair per pair instead of the bin form's two more; which loops
+// take which form was chosen by timing all combinations (the 128-row loop
+// of one-window histograms and the 32-row loop of middle windows gained,
+// the others did not).
+struct WinRaw {
+  unsigned wbase;  // w of the window's first bin (rounding bit 0)
+  unsigned sadjw;  // sadj + bits(2^23)
+  unsigned wl2;    // 2 wl
+  unsigned wo, wi; // this lane's out-of-range and ignore words
+};
+
+__device__ __forceinline__ WinRaw win_raw(unsigned base, unsigned sadj, unsigned wl,
+                                          unsigned vo, unsigned vi) {
+  WinRaw q;
+  q.wbase = 2u * base - 0x4B000000u;
+  q.sadjw = sadj + 0x4B000000u;
+  q.wl2 = 2u * wl;
+  q.wo = q.wbase + 2u * vo;
+  q.wi = q.wbase + 2u * vi;
+  return q;
+}
+
+// The raw form of pair_add_bin for kFull, kFullSafe and kMid.
+template <int kMode>
+__device__ __forceinline__ unsigned pair_add_raw(unsigned &w, bool valid,
+                                                 const WinRaw &q) {
+  static_assert(kMode != kGeneral, "the last window keeps the bin form");
+  bool ignore = !valid;
+  if (kMode == kFullSafe) {
+    w = valid ? w : q.wi;
+  } else if (kMode == kFull) {
+    // bins beyond the spare words all count as out of range: clamp to wo
+    w = valid ? min(w, q.wo) : q.wi;
+  } else {
+    const bool hit = valid && w - q.wbase < q.wl2;
+    w = hit ? w : q.wi;
+    ignore = !hit;
+  }
+  // 1 << (16 * (bin & 1)), the bin's parity being bit 1 of w
+  unsigned inc = 1u << ((w & 2u) << 3);
+  if (ignore) inc = 0u;  // ignore words stay 0
+  unsigned old;
+  asm volatile("atom.shared.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "r"(q.sadjw + (w & ~3u)), "r"(inc));
+  return old;
+}
+
+__device__ __forceinline__ void wrap_check_raw(unsigned old, unsigned w, const WinRaw &q,
+                                               unsigned wl, unsigned vend,
+                                               unsigned long long *gh,
+                                               unsigned long long *oor_total) {
+  const unsigned rot = ((w >> 1) << 4) + 16u;
+  if (__funnelshift_l(old, old, rot) >= 0xFFFF0000u)
+    wrap_fix(old, (w - q.wbase) >> 1, wl, vend, gh, oor_total);
 }
 
 // The column-atom loop of one tile pair for one warp: lanes hold four row
@@ -146,30 +213,45 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
                                           unsigned vo, unsigned vi,
                                           unsigned vend,
                                           unsigned long long *oor_total) {
+  constexpr bool kRaw = kMode == kFull || kMode == kFullSafe;
   const f2 X01 = pk(x[0], x[1]), X23 = pk(x[2], x[3]);
   const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
   const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
   const unsigned uo = vo + base, ui = vi + base;
+  const WinRaw q = win_raw(base, sadj, wl, vo, vi);
   const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
 #pragma unroll 2
   for (int j = 0; j < jend; ++j) {
     const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
     const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
     unsigned u[4], old[4];
-    bins2(X01, Y01, Z01, bx, by, bz, ninv, 0u, u[0], u[1]);
-    bins2(X23, Y23, Z23, bx, by, bz, ninv, 0u, u[2], u[3]);
+    if (kRaw) {
+      bits2(X01, Y01, Z01, bx, by, bz, ninv, u[0], u[1]);
+      bits2(X23, Y23, Z23, bx, by, bz, ninv, u[2], u[3]);
+    } else {
+      bins2(X01, Y01, Z01, bx, by, bz, ninv, 0u, u[0], u[1]);
+      bins2(X23, Y23, Z23, bx, by, bz, ninv, 0u, u[2], u[3]);
+    }
     unsigned any = 0u;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      old[r] = pair_add<kMode>(u[r], kAllValid || j <= jlim[r], base, sadj, wl, kb,
-                               nbins, uo, ui);
+      const bool valid = kAllValid || j <= jlim[r];
+      if constexpr (kRaw)
+        old[r] = pair_add_raw<kMode>(u[r], valid, q);
+      else
+        old[r] = pair_add_bin<kMode>(u[r], valid, base, sadj, wl, kb, nbins, uo, ui);
       any |= old[r];
     }
     // A wrap returns a half at 0xFFFF, so its bit 15 is set: the filter
     // passes only when some counter of these words has reached 32768.
     if (any & 0x80008000u) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) wrap_check(old[r], u[r], base, wl, vend, gh, oor_total);
+      for (int r = 0; r < 4; ++r) {
+        if (kRaw)
+          wrap_check_raw(old[r], u[r], q, wl, vend, gh, oor_total);
+        else
+          wrap_check_bin(old[r], u[r], base, wl, vend, gh, oor_total);
+      }
     }
   }
 }
@@ -186,8 +268,10 @@ __device__ __forceinline__ void pair_loop32(const float4 *__restrict__ bj, int j
                                             unsigned long long *gh, unsigned vo,
                                             unsigned vi, unsigned vend,
                                             unsigned long long *oor_total) {
+  constexpr bool kRaw = kMode == kMid;
   const f2 X = pk(x, x), Y = pk(y, y), Z = pk(z, z);
   const unsigned uo = vo + base, ui = vi + base;
+  const WinRaw q = win_raw(base, sadj, wl, vo, vi);
   const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
 #pragma unroll 2
   for (int j = 0; j < jend; j += 2) {
@@ -195,14 +279,24 @@ __device__ __forceinline__ void pair_loop32(const float4 *__restrict__ bj, int j
     const float4 b1 = __ldg(&bj[kAllValid ? j + 1 : min(j + 1, jend - 1)]);
     const f2 bx = pk(b0.x, b1.x), by = pk(b0.y, b1.y), bz = pk(b0.z, b1.z);
     unsigned u[2], old[2];
-    bins2(X, Y, Z, bx, by, bz, ninv, 0u, u[0], u[1]);
-    old[0] = pair_add<kMode>(u[0], kAllValid || j <= jlim, base, sadj, wl, kb, nbins,
-                             uo, ui);
-    old[1] = pair_add<kMode>(u[1], kAllValid || (j + 1 <= jlim && j + 1 < jend), base,
-                             sadj, wl, kb, nbins, uo, ui);
+    const bool v0 = kAllValid || j <= jlim;
+    const bool v1 = kAllValid || (j + 1 <= jlim && j + 1 < jend);
+    if constexpr (kRaw) {
+      bits2(X, Y, Z, bx, by, bz, ninv, u[0], u[1]);
+      old[0] = pair_add_raw<kMode>(u[0], v0, q);
+      old[1] = pair_add_raw<kMode>(u[1], v1, q);
+    } else {
+      bins2(X, Y, Z, bx, by, bz, ninv, 0u, u[0], u[1]);
+      old[0] = pair_add_bin<kMode>(u[0], v0, base, sadj, wl, kb, nbins, uo, ui);
+      old[1] = pair_add_bin<kMode>(u[1], v1, base, sadj, wl, kb, nbins, uo, ui);
+    }
     if ((old[0] | old[1]) & 0x80008000u) {
-      wrap_check(old[0], u[0], base, wl, vend, gh, oor_total);
-      wrap_check(old[1], u[1], base, wl, vend, gh, oor_total);
+      for (int r = 0; r < 2; ++r) {
+        if (kRaw)
+          wrap_check_raw(old[r], u[r], q, wl, vend, gh, oor_total);
+        else
+          wrap_check_bin(old[r], u[r], base, wl, vend, gh, oor_total);
+      }
     }
   }
 }

@@ -249,6 +249,86 @@ def test_packed_roundf_every_float():
     assert np.all(_kernel_round2_model(big) >= 2 ** 22)
 
 
+def _u32(x):
+    return np.asarray(x).astype(np.uint64) & np.uint64(0xFFFFFFFF)
+
+
+def _pair_add_bin(u, valid, mode, base, sadj, wl, kb, nbins, uo, ui):
+    """The bin form of the tile kernel's pair add (hist.cu pair_add_bin):
+    word address, increment and virtual bin, in uint32 arithmetic."""
+    lk = _u32(u - base)
+    if mode == "safe":
+        u2, ign = np.where(valid, u, ui), ~valid
+    elif mode == "full":
+        u2, ign = np.where(valid, np.minimum(u, uo), ui), ~valid
+    else:  # a middle window
+        hit = valid & (lk < wl)
+        u2, ign = np.where(hit, u, ui), ~hit
+    inc = np.where(ign, 0, np.left_shift(np.uint64(1),
+                                         _u32(u2 << np.uint64(4)) & np.uint64(31)))
+    addr = _u32(sadj + ((u2 >> np.uint64(1)) << np.uint64(2)))
+    return addr, inc, _u32(u2 - base)
+
+
+def _pair_add_raw(w, valid, mode, base, sadj, wl, vo, vi):
+    """The raw-bit form (hist.cu pair_add_raw): w = bits(RD(2p + 8388609))."""
+    wbase = _u32(2 * base - 0x4B000000)
+    sadjw, wl2 = _u32(sadj + 0x4B000000), _u32(2 * wl)
+    wo, wi = _u32(wbase + 2 * vo), _u32(wbase + 2 * vi)
+    if mode == "safe":
+        w2, ign = np.where(valid, w, wi), ~valid
+    elif mode == "full":
+        w2, ign = np.where(valid, np.minimum(w, wo), wi), ~valid
+    else:
+        hit = valid & (_u32(w - wbase) < wl2)
+        w2, ign = np.where(hit, w, wi), ~hit
+    inc = np.where(ign, 0, np.left_shift(np.uint64(1),
+                                         (w2 & np.uint64(2)) << np.uint64(3)))
+    addr = _u32(sadjw + (w2 & np.uint64(0xFFFFFFFC)))
+    return addr, inc, _u32(w2 - wbase) >> np.uint64(1)
+
+
+def test_raw_bit_pair_add_matches_bin_form():
+    """The tile kernel adds a pair either from its bin u = bits(2^23) + bin
+    or from the raw rounding bits w = bits(2^23) + 2 bin + r; both must hit
+    the same counter word and half (and, for the wrap compensation, the
+    same virtual bin) in every mode that uses the raw form, for bins around
+    every window edge and for the bits of NaN and infinite distances."""
+    rng = np.random.default_rng(5)
+    for trial in range(240):
+        mode = ("safe", "full", "mid")[trial % 3]
+        wl = int(rng.integers(1, 114689))
+        nw = (wl + 1) // 2
+        if mode == "mid":
+            kb = int(rng.integers(0, 3_000_000)) & ~1
+            olo = int(rng.integers(0, min(wl, 2000))) & ~1
+        else:
+            kb, olo = 0, 0
+        lane = int(rng.integers(0, 32))
+        vo = 2 * (nw + lane)
+        vi = vo + 64
+        sadj = (int(rng.integers(0, 1 << 14)) * 4
+                - ((0x4B000000 + kb) >> 1) * 4) % (1 << 32)
+        base = 0x4B000000 + kb + olo
+        pkb, pwl = kb + olo, wl - olo
+        pvo, pvi = (vo - olo) % (1 << 32), (vi - olo) % (1 << 32)
+        edges = np.concatenate([pkb + np.arange(-4, 5), pkb + pwl + np.arange(-4, 5),
+                                pkb + pvo + np.arange(-4, 5)])
+        absb = np.concatenate([rng.integers(0, 1 << 22, 2000), edges])
+        absb = absb[(absb >= 0) & (absb < (1 << 22))].astype(np.uint64)
+        r = rng.integers(0, 2, absb.size).astype(np.uint64)
+        w = np.concatenate([np.uint64(0x4B000000) + np.uint64(2) * absb + r,
+                            np.array([0x7FC00000, 0xFFC00000, 0x7F800000,
+                                      0x7F7FFFFF, 0x4B7FFFFF], np.uint64)])
+        u = _u32((w >> np.uint64(1)) + np.uint64(0x25800000))
+        valid = rng.random(w.size) < 0.8
+        a = _pair_add_bin(u, valid, mode, base, sadj, pwl, pkb, None,
+                          _u32(pvo + base), _u32(pvi + base))
+        b = _pair_add_raw(w, valid, mode, base, sadj, pwl, pvo, pvi)
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
+
+
 def test_packed_counter_bookkeeping():
     """Serial model of add16: two 16-bit bins per 32-bit word, wraps and the
     low->high carry compensated in an int64 side array; true counts are
