@@ -214,23 +214,21 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
                                           unsigned vend,
                                           unsigned long long *oor_total) {
   constexpr bool kRaw = kMode == kFull || kMode == kFullSafe;
-  const f2 X01 = pk(x[0], x[1]), X23 = pk(x[2], x[3]);
-  const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
-  const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
   const unsigned uo = vo + base, ui = vi + base;
   const WinRaw q = win_raw(base, sadj, wl, vo, vi);
   const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
 #pragma unroll 2
   for (int j = 0; j < jend; ++j) {
     const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
-    const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
     unsigned u[4], old[4];
-    if (kRaw) {
-      bits2(X01, Y01, Z01, bx, by, bz, ninv, u[0], u[1]);
-      bits2(X23, Y23, Z23, bx, by, bz, ninv, u[2], u[3]);
-    } else {
-      bins2(X01, Y01, Z01, bx, by, bz, ninv, 0u, u[0], u[1]);
-      bins2(X23, Y23, Z23, bx, by, bz, ninv, 0u, u[2], u[3]);
+#pragma unroll
+    for (int h = 0; h < 4; h += 2) {
+      if (kRaw)
+        bits2(x[h], x[h + 1], y[h], y[h + 1], z[h], z[h + 1], b.x, b.x, b.y, b.y, b.z,
+              b.z, ninv, u[h], u[h + 1]);
+      else
+        bins2(x[h], x[h + 1], y[h], y[h + 1], z[h], z[h + 1], b.x, b.x, b.y, b.y, b.z,
+              b.z, ninv, 0u, u[h], u[h + 1]);
     }
     unsigned any = 0u;
 #pragma unroll
@@ -269,7 +267,6 @@ __device__ __forceinline__ void pair_loop32(const float4 *__restrict__ bj, int j
                                             unsigned vi, unsigned vend,
                                             unsigned long long *oor_total) {
   constexpr bool kRaw = kMode == kMid;
-  const f2 X = pk(x, x), Y = pk(y, y), Z = pk(z, z);
   const unsigned uo = vo + base, ui = vi + base;
   const WinRaw q = win_raw(base, sadj, wl, vo, vi);
   const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
@@ -277,16 +274,16 @@ __device__ __forceinline__ void pair_loop32(const float4 *__restrict__ bj, int j
   for (int j = 0; j < jend; j += 2) {
     const float4 b0 = __ldg(&bj[j]);  // warp-uniform: broadcast
     const float4 b1 = __ldg(&bj[kAllValid ? j + 1 : min(j + 1, jend - 1)]);
-    const f2 bx = pk(b0.x, b1.x), by = pk(b0.y, b1.y), bz = pk(b0.z, b1.z);
     unsigned u[2], old[2];
     const bool v0 = kAllValid || j <= jlim;
     const bool v1 = kAllValid || (j + 1 <= jlim && j + 1 < jend);
     if constexpr (kRaw) {
-      bits2(X, Y, Z, bx, by, bz, ninv, u[0], u[1]);
+      bits2(x, x, y, y, z, z, b0.x, b1.x, b0.y, b1.y, b0.z, b1.z, ninv, u[0], u[1]);
       old[0] = pair_add_raw<kMode>(u[0], v0, q);
       old[1] = pair_add_raw<kMode>(u[1], v1, q);
     } else {
-      bins2(X, Y, Z, bx, by, bz, ninv, 0u, u[0], u[1]);
+      bins2(x, x, y, y, z, z, b0.x, b1.x, b0.y, b1.y, b0.z, b1.z, ninv, 0u, u[0],
+            u[1]);
       old[0] = pair_add_bin<kMode>(u[0], v0, base, sadj, wl, kb, nbins, uo, ui);
       old[1] = pair_add_bin<kMode>(u[1], v1, base, sadj, wl, kb, nbins, uo, ui);
     }

@@ -162,17 +162,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       z[r] = a.z;
       jlim[r] = act ? (dtile ? pi : 0x7fffffff) : -1;
     }
-    const f2 X01 = pk(x[0], x[1]), X23 = pk(x[2], x[3]);
-    const f2 Y01 = pk(y[0], y[1]), Y23 = pk(y[2], y[3]);
-    const f2 Z01 = pk(z[0], z[1]), Z23 = pk(z[2], z[3]);
     const float4 *bj = bbase + j0;
 #pragma unroll 2
     for (int j = 0; j < nj; ++j) {
       const float4 b = bj[j];
-      const f2 bx = pk(b.x, b.x), by = pk(b.y, b.y), bz = pk(b.z, b.z);
       unsigned old[4], lk[4];
-      bins2(X01, Y01, Z01, bx, by, bz, ninv, base, lk[0], lk[1]);
-      bins2(X23, Y23, Z23, bx, by, bz, ninv, base, lk[2], lk[3]);
+      bins2(x[0], x[1], y[0], y[1], z[0], z[1], b.x, b.x, b.y, b.y, b.z, b.z, ninv, base,
+            lk[0], lk[1]);
+      bins2(x[2], x[3], y[2], y[3], z[2], z[3], b.x, b.x, b.y, b.y, b.z, b.z, ninv, base,
+            lk[2], lk[3]);
       bool hit[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
