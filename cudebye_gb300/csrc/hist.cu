@@ -217,7 +217,7 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
   const unsigned uo = vo + base, ui = vi + base;
   const WinRaw q = win_raw(base, sadj, wl, vo, vi);
   const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
-#pragma unroll 2
+#pragma unroll 4  // 2: 1-2% slower (spinel_10nm, Gamma sample, 256-model batch)
   for (int j = 0; j < jend; ++j) {
     const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
     unsigned u[4], old[4];
