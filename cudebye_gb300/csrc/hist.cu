@@ -175,8 +175,10 @@ __device__ __forceinline__ unsigned pair_add_raw(unsigned &w, bool valid,
     w = hit ? w : q.wi;
     ignore = !hit;
   }
-  // 1 << (16 * (bin & 1)), the bin's parity being bit 1 of w
-  unsigned inc = 1u << ((w & 2u) << 3);
+  // 1 << (16 * (bin & 1)), the bin's parity being bit 1 of w; as a select
+  // on that bit (a logic op that sets a predicate, and a select) rather
+  // than a computed shift: spinel_10nm histogram 4.20 -> 3.96 ms
+  unsigned inc = (w & 2u) ? 0x10000u : 1u;
   if (ignore) inc = 0u;  // ignore words stay 0
   unsigned old;
   asm volatile("atom.shared.add.u32 %0, [%1], %2;"
