@@ -268,6 +268,32 @@ print("OK")
     assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
 
 
+def test_out_of_range_count_one_window(engine, orc):
+    """One window (rmax half the particle's extent, 1e-3 A bins): the pairs
+    beyond rmax go to the lanes' out-of-range counters by the clamp of the
+    one-window pair loop; the range error reports exactly the oracle's
+    count of them, and the full-range histogram that follows on the same
+    context equals the oracle's bin for bin."""
+    import re
+    m = lattice.spinel(radius=14.0, target=1500, seed=18)
+    nbins = cd.channels(m.rmax / 2, m.rstep)
+    assert nbins < 114688
+    mod = engine.upload(m.xyz, m.counts)
+    try:
+        with pytest.raises(cd.DebyeError) as e:
+            engine.histogram(mod, m.rstep, nbins)
+        assert e.value.code == -7
+        got = int(re.search(r"(\d+) distances", str(e.value)).group(1))
+        _, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, nbins)
+        assert got == bad > 0, (got, bad)
+        h = engine.histogram(mod, m.rstep, m.nbins)
+        want, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins)
+        assert bad == 0
+        np.testing.assert_array_equal(h, want)
+    finally:
+        mod.free()
+
+
 def test_bad_arguments(engine):
     m = engine.upload(np.zeros((2, 3), np.float32), [2])
     stale = cd.Model(engine, m.id, m.counts)
