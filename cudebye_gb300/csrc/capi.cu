@@ -240,7 +240,9 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
   DBX_TRY(dbx::debye_prefactor(sp, m->nspecies, (const double *)c->K.p, nq,
                                (double *)c->ff.p, c->stream, &c->arena));
   c->tm.stop(DBX_T_PREFACTOR, c->stream);
-  if (mode == DBX_DEBYE_TC || mode == DBX_DEBYE_TC3 || mode == DBX_DEBYE_TF32) {
+  const bool tc_form =
+      mode == DBX_DEBYE_TC || mode == DBX_DEBYE_TC3 || mode == DBX_DEBYE_TF32;
+  if (tc_form) {
     std::vector<dbx::TcCol> cols(np);
     for (int p = 0; p < np; ++p) {
       cols[p].hist = m->d_hist + (size_t)p * m->hist_pitch;
@@ -250,9 +252,11 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
     size_t delta = 0;
     const int64_t h0 = c->tc.h2d, d0 = c->tc.d2h;
     c->tc.form = mode == DBX_DEBYE_TC3 ? 1 : mode == DBX_DEBYE_TF32 ? 2 : 0;
-    Error e = dbx::debye_tc(&c->tc, cols, {0, np}, rstep, K,
-                            (const double *)c->K.p, nq, (double *)c->I.p,
-                            c->stream, &delta, &c->tm);
+    Error e = dbx::tc_prepare(&c->tc, cols, {0, np}, rstep, K, (const double *)c->K.p,
+                              nq, c->stream, &delta);
+    if (!e.code)
+      e = dbx::tc_execute(&c->tc, (const double *)c->K.p, (double *)c->I.p, c->stream,
+                          &c->tm);
     c->tc.form = 0;
     c->used += delta;
     c->h2d += c->tc.h2d - h0;
@@ -266,18 +270,46 @@ Error intensity(dbx_ctx *c, dbx::Model *m, double rstep, int64_t nbins,
                               c->stream));
     c->tm.stop(DBX_T_DEBYE, c->stream);
   }
-  if (launched) {  // the histograms' range check, deferred to here
-    c->d2h += sizeof(unsigned long long);
-    Error e = dbx::hist_range_check(c->hws, c->stream);
-    if (e.code) {
-      m->hist_nbins = 0;
-      return e;
+  // What the host reads back — the contraction's wait-timeout word, the
+  // histograms' out-of-range count (the range check deferred to here) and
+  // the intensities — in one round trip through pinned staging, checked in
+  // that order; without pinned memory, one synchronised copy each.
+  const bool oor = launched && c->hws.oor.p;
+  int *h_err = tc_form ? (int *)c->arena.take(sizeof(int)) : nullptr;
+  unsigned long long *h_oor =
+      oor ? (unsigned long long *)c->arena.take(sizeof(unsigned long long)) : nullptr;
+  double *h_I = (double *)c->arena.take(sizeof(double) * nq);
+  c->d2h += (tc_form ? sizeof(int) : 0) + (launched ? sizeof(unsigned long long) : 0) +
+            sizeof(double) * nq;
+  if ((tc_form && !h_err) || (oor && !h_oor) || !h_I) {
+    if (tc_form) DBX_TRY(dbx::tc_check(&c->tc, c->stream));
+    if (launched) {
+      Error e = dbx::hist_range_check(c->hws, c->stream);
+      if (e.code) {
+        m->hist_nbins = 0;
+        return e;
+      }
     }
+    DBX_CUDA_TRY(cudaMemcpyAsync(out_I, c->I.p, sizeof(double) * nq,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    DBX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return dbx::ok();
   }
-  DBX_CUDA_TRY(cudaMemcpyAsync(out_I, c->I.p, sizeof(double) * nq,
-                               cudaMemcpyDeviceToHost, c->stream));
-  c->d2h += sizeof(double) * nq;
+  if (h_err)
+    DBX_CUDA_TRY(cudaMemcpyAsync(h_err, c->tc.err.p, sizeof(int), cudaMemcpyDeviceToHost,
+                                 c->stream));
+  if (h_oor)
+    DBX_CUDA_TRY(cudaMemcpyAsync(h_oor, c->hws.oor.p, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, c->stream));
+  DBX_CUDA_TRY(cudaMemcpyAsync(h_I, c->I.p, sizeof(double) * nq, cudaMemcpyDeviceToHost,
+                               c->stream));
   DBX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (h_err) DBX_TRY(dbx::tc_status(*h_err));
+  if (h_oor && *h_oor) {
+    m->hist_nbins = 0;
+    return dbx::hist_range_error(*h_oor);
+  }
+  std::memcpy(out_I, h_I, sizeof(double) * nq);
   return dbx::ok();
 }
 

@@ -911,25 +911,19 @@ Error tc_combine(const double *d_ff, const double *d_S, int ncols, int nq,
   return ok();
 }
 
+Error tc_status(int herr) {
+  if (herr)
+    return fail(DBX_ERR_TIMEOUT, "tensor-core contraction: a bounded device wait ran out");
+  return ok();
+}
+
 Error tc_check(TcState *st, cudaStream_t stream) {
   int herr = 0;
   DBX_CUDA_TRY(cudaMemcpyAsync(&herr, st->err.p, sizeof(int), cudaMemcpyDeviceToHost,
                                stream));
   DBX_CUDA_TRY(cudaStreamSynchronize(stream));
   st->d2h += sizeof(int);
-  if (herr)
-    return fail(DBX_ERR_TIMEOUT, "tensor-core contraction: a bounded device wait ran out");
-  return ok();
-}
-
-Error debye_tc(TcState *st, std::vector<TcCol> cols,
-               const std::vector<int> &model_col_begin, double rstep,
-               const double *h_K, const double *d_K, int nq, double *d_I,
-               cudaStream_t stream, size_t *delta, Timers *tm) {
-  DBX_TRY(tc_prepare(st, std::move(cols), model_col_begin, rstep, h_K, d_K, nq,
-                     stream, delta));
-  DBX_TRY(tc_execute(st, d_K, d_I, stream, tm));
-  return tc_check(st, stream);
+  return tc_status(herr);
 }
 
 }  // namespace dbx

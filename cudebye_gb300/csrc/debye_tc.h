@@ -14,7 +14,7 @@ struct TcCol {  // one (model, species pair) column of the contraction
   const unsigned long long *hist;  // device counts [nbins]
   long long nbins;
   const double *ff;                // device prefactor [nq]
-  int tile_begin, tile_end;        // filled by debye_tc
+  int tile_begin, tile_end;        // filled by tc_prepare
   double self;                     // self-distance sum, filled on the device
 };
 
@@ -57,11 +57,8 @@ Error tc_combine(const double *d_ff, const double *d_S, int ncols, int nq,
                  double *d_I, cudaStream_t stream);
 // Wait; DBX_ERR_TIMEOUT if a bounded device wait ran out.
 Error tc_check(TcState *st, cudaStream_t stream);
-// prepare + execute + check
-Error debye_tc(TcState *st, std::vector<TcCol> cols,
-               const std::vector<int> &model_col_begin, double rstep,
-               const double *h_K, const double *d_K, int nq, double *d_I,
-               cudaStream_t stream, size_t *bytes_delta, Timers *tm);
+// The status of a contraction from its error word read back by the caller.
+Error tc_status(int herr);
 void tc_release(TcState *st);
 size_t tc_bytes(const TcState *st);
 

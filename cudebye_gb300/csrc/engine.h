@@ -291,6 +291,8 @@ Error hist_plain(const Model &m, int row, int col, float inv_rstep,
 // Wait for the stream; DBX_ERR_RANGE if the last launch binned any pair at
 // k >= nbins.
 Error hist_range_check(const HistWorkspace &scratch, cudaStream_t stream);
+// DBX_ERR_RANGE with the count when oor (out-of-range distances) is not 0.
+Error hist_range_error(unsigned long long oor);
 // upload + launch + range check
 Error hist_run(const HistPlan &plan, float inv_rstep, HistWorkspace *ws,
                cudaStream_t stream, int num_sms, size_t *ws_bytes_delta,

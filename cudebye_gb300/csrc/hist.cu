@@ -1240,17 +1240,21 @@ Error hist_plain(const Model &m, int row, int col, float inv_rstep,
   return ok();
 }
 
+Error hist_range_error(unsigned long long oor) {
+  if (oor)
+    return fail(DBX_ERR_RANGE, std::to_string(oor) +
+                                   " distances bin at or beyond rmax; "
+                                   "increase rmax");
+  return ok();
+}
+
 Error hist_range_check(const HistWorkspace &ws, cudaStream_t stream) {
   unsigned long long oor = 0;
   if (ws.oor.p)
     DBX_CUDA_TRY(cudaMemcpyAsync(&oor, ws.oor.p, sizeof(oor),
                                  cudaMemcpyDeviceToHost, stream));
   DBX_CUDA_TRY(cudaStreamSynchronize(stream));
-  if (oor)
-    return fail(DBX_ERR_RANGE, std::to_string(oor) +
-                                   " distances bin at or beyond rmax; "
-                                   "increase rmax");
-  return ok();
+  return hist_range_error(oor);
 }
 
 Error hist_run(const HistPlan &plan, float inv_rstep, HistWorkspace *ws,
