@@ -414,8 +414,12 @@ Error autotune(dbx_ctx *c, const std::vector<dbx::Model *> &ms, double rstep,
       cudaEventDestroy(b);
     }
   } ev{e0, e1};
+  // several windows per histogram: a segment's window does not start at
+  // bin 0 or ends before the histogram's last bin (small one-window plans
+  // list their items too)
   bool multi = false;
-  for (const dbx::HistSeg &sg : plan.segs) multi |= sg.shape == dbx::kSegList;
+  for (const dbx::HistSeg &sg : plan.segs)
+    multi |= sg.kb != 0 || (unsigned)sg.wl < sg.nbins;
   const int base_tasks = (multi ? 8 : 4) * c->num_sms;
   b.tune = BatchState::Tune{};
   float best = 1e30f;

@@ -673,6 +673,7 @@ void hist_plan_clear(HistPlan *plan) {
   plan->pairs = 0;
   plan->nrows = 0;
   plan->window = 0;
+  plan->quarters = -1;
 }
 
 Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
@@ -707,7 +708,6 @@ Error hist_plan_add(const Model &m, const std::vector<int2> &pairs,
         HistSeg s;
         s.atoms = m.d_atoms;
         s.tiles = m.d_tiles;
-      s.boxes = m.d_boxes;
         s.boxes = m.d_boxes;
         s.out = row;
         s.kb = 0;
@@ -1031,6 +1031,65 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
   int64_t total = 0;
   for (int64_t p : plan->seg_pairs) total += p;
   const size_t S = plan->segs.size();
+  // A small plan of enumerated segments only (one window per histogram)
+  // has too few tile pairs to give every warp of its CTAs one: a warp takes
+  // one tile pair, so a plan of fewer than 16 per task left most warps idle
+  // (a 5,000-atom model: 820 tile pairs over 304 tasks). Such a plan lists
+  // each tile pair as four 32-row items (on a diagonal tile pair, row
+  // quarter rq only over column quarters [0, rq]) and takes about 32 items
+  // per task; the kernel runs them as the 32-row items of a last window,
+  // whose test is exact for a window holding every bin. The decision is
+  // kept for later splits of the plan.
+  if (plan->quarters < 0) {
+    int64_t enum_items = 0;
+    bool all_enum = S > 0;
+    for (size_t s = 0; s < S; ++s) {
+      if (plan->segs[s].shape == kSegList) all_enum = false;
+      else enum_items += plan->seg_items[s].y - plan->seg_items[s].x;
+    }
+    plan->quarters = all_enum && enum_items < 16 * (int64_t)target_tasks ? 1 : 0;
+    if (plan->quarters) {
+      for (size_t s = 0; s < S; ++s) {
+        HistSeg &sg = plan->segs[s];
+        const int begin = (int)plan->items.size();
+        const int count = plan->seg_items[s].y - plan->seg_items[s].x;
+        for (int p = 0; p < count; ++p) {
+          int I, J;
+          bool diag = false;
+          if (sg.shape == kSegRect) {
+            I = sg.ti0 + p / sg.tnj;
+            J = sg.tj0 + p % sg.tnj;
+          } else {  // p = j (j + 1) / 2 + i, i <= j
+            int j = (int)((std::sqrt(8.0 * p + 1.0) - 1.0) * 0.5);
+            while ((int64_t)j * (j + 1) / 2 > p) --j;
+            while ((int64_t)(j + 1) * (j + 2) / 2 <= p) ++j;
+            const int i = p - j * (j + 1) / 2;
+            I = sg.ti0 + i;
+            J = sg.ti0 + j;
+            diag = i == j;
+          }
+          for (int rq = 0; rq < 4; ++rq) {
+            const unsigned q1 = diag ? (unsigned)rq + 1 : 4u;
+            const unsigned x = (unsigned)I | ((4u - q1) << kItemQ1Shift) |
+                               (1u << kItemRowQShift) | ((unsigned)rq << kItemRqShift);
+            plan->items.push_back(
+                make_int2((int)x, J | (diag ? int(0x80000000u) : 0)));
+          }
+        }
+        // equal shares of the segment's pairs: its tasks split by item
+        // count, as for an enumerated segment
+        const int end = (int)plan->items.size();
+        const int64_t share = std::max<int64_t>(1, plan->seg_pairs[s] / std::max(1, end - begin));
+        plan->item_pairs.resize(end, (int)std::min<int64_t>(share, INT32_MAX));
+        sg.shape = kSegList;
+        plan->seg_items[s] = make_int2(begin, end);
+      }
+    }
+  }
+  if (plan->quarters) {
+    target_tasks = (int)std::max<int64_t>(
+        1, std::min<int64_t>(target_tasks, ((int64_t)plan->items.size() + 31) / 32));
+  }
   // Task counts: each segment's share of target_tasks, rounded down, then
   // the largest remainders get one more until the counts sum to exactly
   // target_tasks (each count within [1, the segment's items]). The CTAs
