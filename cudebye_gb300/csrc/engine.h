@@ -227,9 +227,10 @@ struct HistPlan {
   // from sampled tile pairs (kGeomSampled), or forced; not reset by
   // hist_plan_clear
   int geom = 0;
-  // whether the enumerated segments became lists of 32-row items (a small
-  // plan): decided by hist_plan_tasks on its first split of the plan (-1
-  // until then); reset by hist_plan_clear
+  // a plan of enumerated segments only: 1 if they became lists of 32-row
+  // items (a small plan), 2 if not; 0 for a plan with listed segments;
+  // decided by hist_plan_tasks on its first split of the plan (-1 until
+  // then); reset by hist_plan_clear
   int quarters = -1;
   int64_t pairs = 0;           // binned pairs (the reference's "Distances
                                // Expected" summed over the selected pairs)

@@ -1049,8 +1049,9 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
     }
     // 8: a 4,477-atom model's histogram 0.070 -> 0.045 ms with the 32-row
     // items, a 12,004-atom model's (15 tile pairs per task) 0.088 -> 0.096
-    plan->quarters = all_enum && enum_items < 8 * (int64_t)target_tasks ? 1 : 0;
-    if (plan->quarters) {
+    plan->quarters =
+        !all_enum ? 0 : (enum_items < 8 * (int64_t)target_tasks ? 1 : 2);
+    if (plan->quarters == 1) {
       for (size_t s = 0; s < S; ++s) {
         HistSeg &sg = plan->segs[s];
         const int begin = (int)plan->items.size();
@@ -1088,9 +1089,15 @@ void hist_plan_tasks(HistPlan *plan, int target_tasks) {
       }
     }
   }
-  if (plan->quarters) {
-    target_tasks = (int)std::max<int64_t>(
-        1, std::min<int64_t>(target_tasks, ((int64_t)plan->items.size() + 31) / 32));
+  // A plan of enumerated tile pairs (or their 32-row items) takes at least
+  // 32 items per task where it has them: a CTA runs its task's items one
+  // per warp, so two tasks of 15 items on one SM took two item times where
+  // one task of 30 takes one (12,004 atoms: 4,560 tile pairs).
+  if (plan->quarters > 0) {
+    int64_t items = 0;
+    for (size_t s = 0; s < S; ++s) items += plan->seg_items[s].y - plan->seg_items[s].x;
+    target_tasks =
+        (int)std::max<int64_t>(1, std::min<int64_t>(target_tasks, (items + 31) / 32));
   }
   // Task counts: each segment's share of target_tasks, rounded down, then
   // the largest remainders get one more until the counts sum to exactly
