@@ -6,11 +6,13 @@
 //
 // Design:
 //  * Atoms of each species are sorted along a Hilbert curve and cut into
-//    tiles of 128 (model.cu, spatial_sort.cu); a work item is one tile pair.
+//    tiles of 128 (model.cu, spatial_sort.cu); a work item is one tile pair,
+//    or one 32-row quarter of it (listed for multi-window histograms and
+//    small plans).
 //  * A CTA owns a window of up to ~114k bins held in shared memory as packed
 //    16-bit counters (two bins per 32-bit word). A counter that wraps is
 //    detected from the atomic's return value and compensated exactly in the
-//    int64 global histogram (see wrap16), so the counts stay exact.
+//    int64 global histogram (wrap_fix), so the counts stay exact.
 //  * Tile pairs are grouped into (species pair, bin window) segments from
 //    their bounding boxes, and split into equal CTA tasks. Each task writes
 //    its packed window once to a scratch slot; a reduce kernel sums the slots
@@ -218,7 +220,7 @@ __device__ __forceinline__ void pair_loop(const float4 *__restrict__ bj,
   constexpr bool kRaw = kMode == kFull || kMode == kFullSafe;
   const unsigned uo = vo + base, ui = vi + base;
   const WinRaw q = win_raw(base, sadj, wl, vo, vi);
-  const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
+  const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bits2 / bins2 take -2 inv
 #pragma unroll 4  // 2: 1-2% slower (spinel_10nm, Gamma sample, 256-model batch)
   for (int j = 0; j < jend; ++j) {
     const float4 b = __ldg(&bj[j]);  // warp-uniform: broadcast
@@ -271,7 +273,7 @@ __device__ __forceinline__ void pair_loop32(const float4 *__restrict__ bj, int j
   constexpr bool kRaw = kMode == kMid;
   const unsigned uo = vo + base, ui = vi + base;
   const WinRaw q = win_raw(base, sadj, wl, vo, vi);
-  const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bins2 takes -2 inv
+  const f2 ninv = pk(-2.0f * inv, -2.0f * inv);  // bits2 / bins2 take -2 inv
 #pragma unroll 2
   for (int j = 0; j < jend; j += 2) {
     const float4 b0 = __ldg(&bj[j]);  // warp-uniform: broadcast
