@@ -268,6 +268,34 @@ print("OK")
     assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
 
 
+def test_pattern_range_error_then_pattern(engine, orc):
+    """A full pattern whose rmax is below the particle's extent: dbx_pattern
+    reads back the histograms' out-of-range count with the intensities and
+    returns DBX_ERR_RANGE with the oracle's count; the model's histograms are
+    not kept, and a pattern with enough bins that follows on the same
+    context and model equals the FP64 oracle's within 1e-6."""
+    import re
+    m = lattice.spinel(radius=12.0, target=1200, seed=19)
+    tt, K = m.k_grid()
+    K = K[::20]
+    nbins = cd.channels(m.rmax / 2, m.rstep)
+    mod = engine.upload(m.xyz, m.counts)
+    try:
+        with pytest.raises(cd.DebyeError) as e:
+            engine.pattern(mod, m.rstep, nbins, m.species, K)
+        assert e.value.code == -7
+        got = int(re.search(r"(\d+) distances", str(e.value)).group(1))
+        _, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, nbins)
+        assert got == bad > 0, (got, bad)
+        I = engine.pattern(mod, m.rstep, m.nbins, m.species, K)
+        want_h, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins)
+        assert bad == 0
+        want = orc.intensity(K, want_h, m.species, m.rstep)
+        assert float(np.max(np.abs(I - want) / np.abs(want))) <= 1e-6
+    finally:
+        mod.free()
+
+
 def test_out_of_range_count_one_window(engine, orc):
     """One window (rmax half the particle's extent, 1e-3 A bins): the pairs
     beyond rmax go to the lanes' out-of-range counters by the clamp of the
