@@ -165,3 +165,34 @@ def test_tf32_split_form(engine, orc):
     assert rel32.max() <= 1e-4, (rel32.max(), rel3.max(), rel.max())
     assert rel32.max() < rel3.max(), (rel32.max(), rel3.max())
     assert rel.max() <= rel32.max()
+
+
+def test_patterns_on_a_caller_stream(engine, orc):
+    """dbx_set_stream: patterns launched on a caller's stream equal those on
+    the context's own stream bit for bit and the FP64 oracle within 1e-6,
+    for a small model (whose prefactors run on the context's second stream,
+    joined back into the caller's) and a larger one (in stream order)."""
+    torch = pytest.importorskip("torch")
+    small = lattice.plain_small()
+    large = lattice.spinel(radius=20.0, target=25000, seed=23)
+    tt, K = small.k_grid()
+    K = K[::15]
+    s = torch.cuda.Stream(device=torch.device("cuda", 0))
+    for m in (small, large):
+        mod = engine.upload(m.xyz, m.counts)
+        try:
+            own = engine.pattern(mod, m.rstep, m.nbins, m.species, K)
+            engine.set_stream(s.cuda_stream)
+            try:
+                mine = [engine.pattern(mod, m.rstep, m.nbins, m.species, K).copy()
+                        for _ in range(3)]
+            finally:
+                engine.set_stream(None)
+            for I in mine:
+                np.testing.assert_array_equal(I, own)
+            h, bad = orc.model_histograms(m.xyz, m.counts, m.rstep, m.nbins)
+            assert bad == 0
+            want = orc.intensity(K, h, m.species, m.rstep)
+            assert float(np.max(np.abs(own - want) / np.abs(want))) <= 1e-6
+        finally:
+            mod.free()
