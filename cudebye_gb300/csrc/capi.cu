@@ -827,7 +827,7 @@ int model_upload(dbx_ctx *c, const float *x, const float *y, const float *z,
     return set_err(c, dbx::fail(DBX_ERR_NOMEM, "HBM budget exceeded by model"));
   if (natoms >= dev_min) {
     e = dbx::model_upload_sorted(m.get(), x, y, z, xyz, counts, nspecies,
-                                 (float *)c->pin, c->stream);
+                                 (float *)c->pin, c->pin_cap * sizeof(float4), c->stream);
   } else {
     std::vector<float> planes;  // small models: de-interleaved on the host
     if (xyz) {

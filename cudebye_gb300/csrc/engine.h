@@ -147,13 +147,14 @@ Error model_to_device(Model *m, const float4 *atoms, cudaStream_t stream,
 size_t model_device_bytes(const Model &m);  // atoms, tiles, hist, plan
 // Sort and upload on the device (spatial_sort.cu): the same atoms, tiles and
 // boxes as model_prepare + model_to_device; `pin` is pinned host memory
-// of at least 3 natoms floats; the tile boxes stay on the device
+// of pin_bytes >= 12 natoms bytes (the coordinates; small arrays go
+// through the rest where it fits); the tile boxes stay on the device
 // (d_boxes) until model_host_boxes copies them for a multi-window plan.
 // Coordinates as SoA planes x, y, z, or (xyz not null) one interleaved
 // [natoms][3] array. For natoms > 0.
 Error model_upload_sorted(Model *m, const float *x, const float *y, const float *z,
                           const float *xyz, const int64_t *counts, int nspecies,
-                          float *pin, cudaStream_t stream);
+                          float *pin, size_t pin_bytes, cudaStream_t stream);
 Error model_host_boxes(Model *m, cudaStream_t stream);
 void model_release(Model *m);
 // The same, device arrays freed in `stream` order (no device-wide wait);

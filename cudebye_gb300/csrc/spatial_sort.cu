@@ -273,7 +273,7 @@ __global__ void deinterleave_kernel(const float *__restrict__ aos, long long n,
 
 Error model_upload_sorted(Model *m, const float *x, const float *y, const float *z,
                           const float *xyz, const int64_t *counts, int nspecies,
-                          float *pin, cudaStream_t st) {
+                          float *pin, size_t pin_bytes, cudaStream_t st) {
   int64_t natoms = 0;
   for (int s = 0; s < nspecies; ++s) natoms += counts[s];
   const long long n = natoms;
@@ -303,15 +303,6 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
   const int ntiles = (int)m->tiles.size();
   const size_t abytes = sizeof(float4) * n, tbytes = sizeof(int2) * std::max(ntiles, 1),
                bbytes = sizeof(TileBox) * std::max(ntiles, 1);
-  // raw coordinates through the pinned staging (3n floats), as given: SoA
-  // planes, or one interleaved array de-interleaved on the device
-  if (xyz) {
-    std::memcpy(pin, xyz, sizeof(float) * 3 * n);
-  } else {
-    std::memcpy(pin, x, sizeof(float) * n);
-    std::memcpy(pin + n, y, sizeof(float) * n);
-    std::memcpy(pin + 2 * n, z, sizeof(float) * n);
-  }
   const long long nblk = (n + kSortChunk - 1) / kSortChunk;
   float *d_xyz = nullptr, *d_aos = nullptr;
   unsigned long long *k1 = nullptr, *k2 = nullptr;
@@ -357,24 +348,54 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
       lohi0[s * 6 + d] = 0xFFFFFFFFu;
       lohi0[s * 6 + 3 + d] = 0u;
     }
-  e = cudaMemcpyAsync(xyz ? d_aos : d_xyz, pin, sizeof(float) * 3 * n,
-                      cudaMemcpyHostToDevice, st);
+  // Raw coordinates through the pinned staging (3n floats), as given: SoA
+  // planes, or one interleaved array de-interleaved on the device. They are
+  // staged in pieces, each piece's copy queued as soon as it is staged, so
+  // the transfer overlaps the staging of the rest.
+  const long long nf = 3 * n;
+  const long long piece = std::max<long long>(1 << 16, (nf + 3) / 4);
+  float *dst = xyz ? d_aos : d_xyz;
+  for (long long a = 0; a < nf && e == cudaSuccess; a += piece) {
+    const long long b = std::min(nf, a + piece);
+    if (xyz) {
+      std::memcpy(pin + a, xyz + a, sizeof(float) * (b - a));
+    } else {  // the planes end to end: x, y, z
+      for (long long i = a; i < b;) {
+        const int plane = (int)(i / n);
+        const long long j = std::min(b, (long long)(plane + 1) * n);
+        const float *src = plane == 0 ? x : (plane == 1 ? y : z);
+        std::memcpy(pin + i, src + (i - plane * n), sizeof(float) * (j - i));
+        i = j;
+      }
+    }
+    e = cudaMemcpyAsync(dst + a, pin + a, sizeof(float) * (b - a),
+                        cudaMemcpyHostToDevice, st);
+  }
   if (e == cudaSuccess && xyz) {
     deinterleave_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_aos, n, d_xyz);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(lohi, lohi0.data(), sizeof(unsigned) * lohi0.size(),
-                        cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_start, start.data(), sizeof(long long) * start.size(),
-                        cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_bits, bits.data(), sizeof(int) * nspecies,
-                        cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(m->d_tiles, m->tiles.data(), sizeof(int2) * ntiles,
-                        cudaMemcpyHostToDevice, st);
+  // The small arrays through the rest of the staging, after the
+  // coordinates, where they fit: a copy from pageable memory could wait for
+  // the stream.
+  {
+    char *tail = reinterpret_cast<char *>(pin) + ((12 * n + 15) & ~15LL);
+    char *const end = reinterpret_cast<char *>(pin) + pin_bytes;
+    auto put = [&](void *d, const void *h, size_t bytes) {
+      if (e != cudaSuccess || bytes == 0) return;
+      const void *from = h;
+      if (tail + bytes <= end) {
+        std::memcpy(tail, h, bytes);
+        from = tail;
+        tail += (bytes + 15) & ~size_t(15);
+      }
+      e = cudaMemcpyAsync(d, from, bytes, cudaMemcpyHostToDevice, st);
+    };
+    put(lohi, lohi0.data(), sizeof(unsigned) * lohi0.size());
+    put(d_start, start.data(), sizeof(long long) * start.size());
+    put(d_bits, bits.data(), sizeof(int) * nspecies);
+    put(m->d_tiles, m->tiles.data(), sizeof(int2) * ntiles);
+  }
   if (e == cudaSuccess) {
     const unsigned g = (unsigned)((n + 255) / 256);
     bbox_kernel<<<dim3(std::min<unsigned>(g, 64u), nspecies), 256, 0, st>>>(
