@@ -73,12 +73,13 @@ __global__ void bbox_kernel(const float *__restrict__ xyz, long long n,
   }
 }
 
-// Sort key of every atom: bits 32.. the species, bits 0..31 the code
-// computed exactly as the host does (FP32, IEEE operations).
+// Sort key of every atom: bits code_shift.. the species, bits below the
+// code computed exactly as the host does (FP32, IEEE operations), so the
+// radix passes cover the code's bits and the species' bits with no gap.
 __global__ void keys_kernel(const float *__restrict__ xyz, long long n,
                             const long long *__restrict__ start, int ns,
                             const unsigned *__restrict__ lohi,
-                            const int *__restrict__ bits,
+                            const int *__restrict__ bits, int code_shift,
                             unsigned long long *__restrict__ key,
                             int *__restrict__ idx) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -101,7 +102,7 @@ __global__ void keys_kernel(const float *__restrict__ xyz, long long n,
     q[d] = (uint32_t)t;
   }
   const uint32_t code = hilbert3(q[0], q[1], q[2], bits[s]);
-  key[i] = ((unsigned long long)s << 32) | code;
+  key[i] = ((unsigned long long)s << code_shift) | code;
   idx[i] = (int)(i - start[s]);
 }
 
@@ -201,11 +202,11 @@ __global__ void radix_scatter_kernel(const unsigned long long *__restrict__ key,
 __global__ void gather_kernel(const float *__restrict__ xyz, long long n,
                               const long long *__restrict__ start, int ns,
                               const unsigned long long *__restrict__ key,
-                              const int *__restrict__ idx,
+                              int code_shift, const int *__restrict__ idx,
                               float4 *__restrict__ atoms) {
   const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (j >= n) return;
-  const int s = (int)(key[j] >> 32);
+  const int s = (int)(key[j] >> code_shift);
   const long long src = start[s] + idx[j];
   atoms[j] = make_float4(xyz[src], xyz[n + src], xyz[2 * n + src], 0.f);
 }
@@ -400,17 +401,17 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
     const unsigned g = (unsigned)((n + 255) / 256);
     bbox_kernel<<<dim3(std::min<unsigned>(g, 64u), nspecies), 256, 0, st>>>(
         d_xyz, n, d_start, nspecies, lohi);
-    keys_kernel<<<g, 256, 0, st>>>(d_xyz, n, d_start, nspecies, lohi, d_bits, k1, i1);
-    // digits: the code bits, then the species bits (a stable sort by code,
-    // then by species: species-major, code order within, ties in input
-    // order)
+    // digits over the code bits and the species bits above them (a stable
+    // LSD sort: species-major, code order within, ties in input order);
+    // the species share the code's last digit where it has room
     int code_bits = 0;
     for (int b : bits) code_bits = std::max(code_bits, 3 * b);
     int sp_bits = 0;
     while ((1 << sp_bits) < nspecies) ++sp_bits;
+    keys_kernel<<<g, 256, 0, st>>>(d_xyz, n, d_start, nspecies, lohi, d_bits, code_bits,
+                                   k1, i1);
     std::vector<int> shifts;
-    for (int sh = 0; sh < code_bits; sh += 8) shifts.push_back(sh);
-    for (int sh = 0; sh < sp_bits; sh += 8) shifts.push_back(32 + sh);
+    for (int sh = 0; sh < code_bits + sp_bits; sh += 8) shifts.push_back(sh);
     for (int sh : shifts) {
       radix_count_kernel<<<(unsigned)nblk, kSortThreads, 0, st>>>(k1, n, sh, cnt);
       radix_scan_kernel<<<1, 1024, 0, st>>>(cnt, (long long)kRadix * nblk);
@@ -419,7 +420,8 @@ Error model_upload_sorted(Model *m, const float *x, const float *y, const float 
       std::swap(k1, k2);
       std::swap(i1, i2);
     }
-    gather_kernel<<<g, 256, 0, st>>>(d_xyz, n, d_start, nspecies, k1, i1, m->d_atoms);
+    gather_kernel<<<g, 256, 0, st>>>(d_xyz, n, d_start, nspecies, k1, code_bits, i1,
+                                     m->d_atoms);
     tile_boxes_kernel<<<(unsigned)((ntiles * 32LL + 255) / 256), 256, 0, st>>>(
         m->d_atoms, m->d_tiles, ntiles, m->d_boxes);
     e = cudaGetLastError();
